@@ -1,0 +1,367 @@
+"""Throughput of the nbfmm hot path on GB300: Stars::update steps (solve + Stormer-Verlet + prune).
+
+Default workload: two colliding disks, N = 16,777,216, depth 9 (num_level 8, 512 x 512 leaf cells), eps 5e-4,
+dt 5e-5 (seeded synthetic particles). One step = one reference Stars::update (update.cu:47-55). Prints one JSON
+line (metric particle-steps/s). `--impl reference` times the reference's algorithm on the host cores instead
+(the oracle's CPU restatement; the reference itself has no CPU path), on a bounded sample of the workload.
+
+Multi-GPU (torchrun): every rank steps its own replica of the workload (the path has no exchange step);
+value = all particles stepped on all ranks / max-over-ranks time.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+FLOP_PER_PAIR = 15  # 2 sub, 3 for r^2, 1 sqrt, 1 for r*r^2 (+eps fused: 2), 1 rcp, 1 mul by m, 4 for 2 FMAs
+SMS, FP32_LANES, MUFU_LANES = 152, 128, 16
+WINDOW_CELLS = 32  # side of the CPU sample window, in leaf cells
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--config", default="two_disks_16m")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def workload_name(sysm):
+    depth = sysm.num_level + 1
+    b = 1 << depth
+    return (f"{sysm.name}: N={sysm.n:,}, depth {depth} ({b}x{b} leaf cells), eps {sysm.epsilon:g}, "
+            f"dt {sysm.dt:g}, G {sysm.grav_const:g}, limits {list(sysm.limits)}")
+
+
+# ---- CPU side (oracle = the reference's algorithm restated on the host) --------------------------------------
+
+def window_sample(sysm):
+    """A WINDOW_CELLS x WINDOW_CELLS leaf-cell window of the system at full density: same cell size and
+    particles per cell as the full workload, so the cost per particle-step matches it."""
+    b = 1 << (sysm.num_level + 1)
+    cell = (sysm.limits[2] - sysm.limits[0]) / b
+    side = WINDOW_CELLS * cell
+    # centre the window on the disk material: the median position of a seeded subset
+    rng = np.random.default_rng(0)
+    sub = sysm.position[rng.choice(sysm.n, min(sysm.n, 4096), replace=False)]
+    cx, cy = float(np.median(sub[:, 0])), float(np.median(sub[:, 1]))
+    if sysm.name == "two_disks":
+        cx, cy = -0.35, 0.0  # on the ring of the left disk, away from its centre mass
+    lim = (cx - side / 2, cy - side / 2, cx + side / 2, cy + side / 2)
+    p = sysm.position
+    m = (p[:, 0] >= lim[0]) & (p[:, 0] < lim[2]) & (p[:, 1] >= lim[1]) & (p[:, 1] < lim[3])
+    level = int(np.log2(WINDOW_CELLS)) - 1
+    prev = sysm.previous()
+    return p[m].copy(), prev[m].copy(), sysm.weight[m].copy(), lim, level
+
+
+def cpu_steps(sysm, steps, budget_s=None):
+    """Steps the window sample with the oracle's Stars::update; returns (particle-steps/s, threads, n, steps)."""
+    from oracle import oracle
+
+    cur, prev, w, lim, level = window_sample(sysm)
+    n = len(w)
+    tick = sysm.tick()
+    done, t0 = 0, time.perf_counter()
+    while True:
+        k, cur[:n], prev[:n], w[:n], _ = oracle.stars_update(cur[:n], prev[:n], w[:n], level, lim, sysm.epsilon, tick)
+        done += n
+        n = k
+        steps -= 1
+        el = time.perf_counter() - t0
+        if steps <= 0 or (budget_s is not None and el >= budget_s):
+            break
+    return done / el, oracle.num_threads(), len(w), el
+
+
+def cpu_sample_text(sysm, n, steps):
+    return (f"{steps} oracle Stars::update steps of a {WINDOW_CELLS}x{WINDOW_CELLS}-leaf-cell window of the "
+            f"workload ({n:,} particles at full density, same cell size, num_level "
+            f"{int(np.log2(WINDOW_CELLS)) - 1}), OpenMP over the host cores")
+
+
+def run_reference_arm(args, sysm, rank):
+    if rank != 0:
+        return
+    from oracle import oracle
+
+    oracle.lib()
+    cur, prev, w, lim, level = window_sample(sysm)
+    n0 = len(w)
+    tick = sysm.tick()
+    n = n0
+    for _ in range(args.warmup):
+        n, cur[:n], prev[:n], w[:n], _ = oracle.stars_update(cur[:n], prev[:n], w[:n], level, lim, sysm.epsilon, tick)
+    done, t0 = 0, time.perf_counter()
+    for _ in range(args.steps):
+        k, cur[:n], prev[:n], w[:n], _ = oracle.stars_update(cur[:n], prev[:n], w[:n], level, lim, sysm.epsilon, tick)
+        done += n
+        n = k
+    el = time.perf_counter() - t0
+    v = done / el
+    out = {
+        "impl": "reference", "metric": "particle-steps/s", "value": v, "unit": "particle-steps/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": el * 1e3 / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded)",
+        "config": {"workload": workload_name(sysm), "sample_particles": n0, "parallelism": "host threads"},
+        "cpu_baseline": {"value": v, "unit": "particle-steps/s", "cores": oracle.num_threads(), "kind": "port",
+                         "sample": cpu_sample_text(sysm, n0, args.steps)},
+        "e2e": {"value": v, "unit": "particle-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(out), flush=True)
+
+
+# ---- GPU side --------------------------------------------------------------------------------------------------
+
+class ClockSampler:
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_id):
+        self.proc = None
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", device_id, "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        out, _ = self.proc.communicate(timeout=10)
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in out.splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 8:
+                continue
+            try:
+                sm.append(float(f[0]))
+                mx.append(float(f[1]))
+            except ValueError:
+                continue
+            for name, val in zip(names, f[4:8]):
+                if val.lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_sm_mhz():
+    """Median SM clock under load recorded in MEASURED_PEAKS.json, when the run sampled none itself."""
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        return float(json.load(open(path))["clocks_under_load"]["sm_mhz_median"])
+    except (OSError, KeyError, ValueError):
+        return 1900.0
+
+
+def p2p_pairs(torch, head, base_dim):
+    """Algorithmic P2P pair count of one solve: each target against its 3x3 leaf cells, self excluded."""
+    n = (head[1:base_dim * base_dim + 1] - head[:base_dim * base_dim]).double().reshape(1, 1, base_dim, base_dim)
+    ns = torch.nn.functional.conv2d(n, torch.ones(1, 1, 3, 3, dtype=n.dtype, device=n.device), padding=1)
+    return int((n * (ns - 1)).clamp(min=0).sum().item())
+
+
+def fp64_error(torch, pos, w, eff, eps, targets):
+    """Relative error of the engine's effects against the FP64 all-pairs direct sum, on the GPU, for targets."""
+    p = pos.double()
+    m = w.double()
+    errs = []
+    for t in targets.split(8):
+        d = p[None, :, :] - p[t][:, None, :]  # (8, n, 2)
+        r = torch.sqrt((d * d).sum(-1))
+        s = m[None, :] / (r * r * r + eps)
+        s[torch.arange(len(t), device=p.device), t] = 0.0
+        ref = (d * s[..., None]).sum(1)
+        errs.append(torch.linalg.norm(eff[t].double() - ref, dim=1) / torch.linalg.norm(ref, dim=1))
+    e = torch.cat(errs)
+    return {"median": float(e.median()), "p99": float(torch.quantile(e, 0.99)), "max": float(e.max()),
+            "targets": int(len(targets))}
+
+
+def main():
+    args = parse()
+    from nbfmm_gb300 import workloads
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    sysm = workloads.CONFIGS[args.config]()
+
+    if args.impl == "reference":
+        run_reference_arm(args, sysm, rank)
+        return
+
+    import torch
+
+    import nbfmm_gb300
+
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    dev_id = str(local)
+    try:
+        dev_id = "GPU-" + str(torch.cuda.get_device_properties(local).uuid)
+    except Exception:
+        pass
+
+    n = sysm.n
+    pos = torch.from_numpy(sysm.position).cuda()
+    w = torch.from_numpy(sysm.weight).cuda()
+    prev = torch.from_numpy(sysm.previous()).cuda()
+
+    # One solve of the initial state: the P2P pair count and the error against the FP64 direct sum.
+    solver = nbfmm_gb300.Solver(sysm.num_level, n, sysm.limits, epsilon=sysm.epsilon)
+    eff = torch.empty(n, 2, device="cuda")
+    solver.solve(n, pos, w, eff)
+    torch.cuda.synchronize()
+    b = 1 << (sysm.num_level + 1)
+    pairs0 = p2p_pairs(torch, solver.buffers()["head"], b)
+    g = torch.Generator(device="cpu").manual_seed(1234)
+    targets = torch.randperm(n, generator=g)[:512].cuda()
+    err64 = fp64_error(torch, pos, w, eff, sysm.epsilon, targets)
+    del eff
+
+    stars = nbfmm_gb300.Stars(sysm.num_level, n, tick=sysm.dt, grav_const=sysm.grav_const,
+                              position_limits=sysm.limits, epsilon=sysm.epsilon)
+    stars.gpuptr_position_cur_.copy_(pos)
+    stars.gpuptr_position_pre_.copy_(prev)
+    stars.gpuptr_weight_.copy_(w)
+    stream = torch.cuda.current_stream()
+    stars.update(args.warmup)
+    torch.cuda.synchronize()
+
+    # ---- timed region: K steps in one update call, P2P timed per launch with CUDA events ----
+    stars.profile_begin(args.steps)
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    clocks = ClockSampler(dev_id)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    stars.update(args.steps)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    elapsed_ms = ev0.elapsed_time(ev1)
+    p2p_ms, p2p_launches = stars.profile_end()
+    if dist:
+        t = torch.tensor([elapsed_ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        elapsed_ms = float(t.item())
+    n_end = stars.num_star_
+
+    # Pair count at the end of the timed steps (the system moves); the roofline uses the mean of both ends.
+    cur_now = stars.gpuptr_position_cur_[:n_end].clone()
+    solver.solve(n_end, cur_now, stars.gpuptr_weight_[:n_end].clone(), torch.empty(n_end, 2, device="cuda"))
+    torch.cuda.synchronize()
+    pairs1 = p2p_pairs(torch, solver.buffers()["head"], b)
+    pairs = 0.5 * (pairs0 + pairs1)
+
+    # ---- e2e: the public API with host buffers; every step copies the state in and out ----
+    e2e_steps = args.steps
+    h_cur = torch.empty(n_end, 2, pin_memory=True)
+    h_prev = torch.empty(n_end, 2, pin_memory=True)
+    h_w = torch.empty(n_end, pin_memory=True)
+    h_cur.copy_(stars.gpuptr_position_cur_[:n_end])
+    h_prev.copy_(stars.gpuptr_position_pre_[:n_end])
+    h_w.copy_(stars.gpuptr_weight_[:n_end])
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(e2e_steps):
+        stars.gpuptr_position_cur_[:n_end].copy_(h_cur, non_blocking=True)
+        stars.gpuptr_position_pre_[:n_end].copy_(h_prev, non_blocking=True)
+        stars.gpuptr_weight_[:n_end].copy_(h_w, non_blocking=True)
+        stars.update(1)
+        h_cur.copy_(stars.gpuptr_position_cur_[:n_end], non_blocking=True)
+        h_prev.copy_(stars.gpuptr_position_pre_[:n_end], non_blocking=True)
+        h_w.copy_(stars.gpuptr_weight_[:n_end], non_blocking=True)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    e2e_ms = e0.elapsed_time(e1)
+    if dist:
+        t = torch.tensor([e2e_ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_ms = float(t.item())
+    io_bytes = n_end * (8 + 8 + 4)
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        v, cores, ns, el = cpu_steps(sysm, 1000, budget_s=15.0)
+        steps_done = max(1, int(round(v * el / max(ns, 1))))
+        cpu = {"value": v, "unit": "particle-steps/s", "cores": cores, "kind": "port",
+               "sample": cpu_sample_text(sysm, ns, steps_done)}
+
+    if rank != 0:
+        return
+    value = n * args.steps * world / (elapsed_ms / 1e3)
+    p2p_s = p2p_ms / max(p2p_launches, 1) / 1e3
+    sm_mhz = clk["sm_mhz"] or measured_sm_mhz()
+    fp32_peak = SMS * FP32_LANES * 2 * sm_mhz * 1e6 / 1e12
+    achieved = FLOP_PER_PAIR * pairs / p2p_s / 1e12
+    out = {
+        "metric": "particle-steps/s",
+        "value": value,
+        "unit": "particle-steps/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": elapsed_ms / args.steps,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32",
+        "data": "synthetic (seeded; nbfmm_gb300/workloads.py)",
+        "config": {"workload": workload_name(sysm), "N": n, "num_level": sysm.num_level,
+                   "steps_per_call": args.steps, "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
+                   "l2": "inputs larger than L2 (state + sorted copy ~ 0.9 GB at N=16.8M)",
+                   "stars_after_timed_steps": n_end},
+        "roofline": {
+            "kernel": "p2p_kernel<kVerlet> (near field + L2P + Verlet epilogue)",
+            "bound": "fp32", "unit": "TFLOP/s",
+            "achieved": achieved, "peak": fp32_peak, "frac": achieved / fp32_peak, "traffic": None,
+            "peak_source": f"nominal FP32 FMA rate {SMS} SMs x {FP32_LANES} lanes x 2 at the median sampled SM clock "
+                           f"({sm_mhz:.0f} MHz); MEASURED_PEAKS.json has no SIMT FP32 figure",
+            "flop_per_pair": FLOP_PER_PAIR, "pairs_per_launch": pairs, "p2p_ms_per_launch": p2p_s * 1e3,
+            "p2p_share_of_step": p2p_ms / max(elapsed_ms, 1e-9),
+            "pairs_per_s": pairs / p2p_s,
+            "mufu_bound_pairs_per_s": SMS * MUFU_LANES * sm_mhz * 1e6 / 2,
+        },
+        "e2e": {"value": n_end * e2e_steps * world / (e2e_ms / 1e3), "unit": "particle-steps/s",
+                "h2d_bytes_per_step": io_bytes, "d2h_bytes_per_step": io_bytes,
+                "api": "Stars.update(1) per step, state copied in from and out to pinned host memory"},
+        "cpu_baseline": cpu,
+        "gpu_launches": stars.kernel_launches(args.steps),
+        "clocks": clk,
+        "error_vs_fp64": err64,
+    }
+    print(json.dumps(out), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

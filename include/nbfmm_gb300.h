@@ -1,0 +1,138 @@
+/*
+ * nbfmm_gb300.h -- C ABI of the GB300-native nbfmm engine (libnbfmm_gb300.so).
+ *
+ * Drop-in for the hot path of emfomy/nbfmm: nbfmm::Solver (include/nbfmm/core/solver.hpp) and the update
+ * path of nbfmm::Stars (include/nbfmm/display/stars.hpp). All pointers named gpuptr_* are device pointers
+ * in the reference's layouts: positions and effects are float2 arrays given as float* of 2*n floats,
+ * weights are float arrays of n floats, limits are {x_min, y_min, x_max, y_max} (the reference's float4).
+ * Streams are cudaStream_t passed as void* (NULL = legacy default stream). Every call returns NBFMM_OK or
+ * an error code and leaves a message for nbfmm_last_error(); no call aborts the process. Calls on one
+ * handle must not overlap (a handle owns its workspace, as the reference's Solver does).
+ */
+#ifndef NBFMM_GB300_H_
+#define NBFMM_GB300_H_
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define NBFMM_GB300_VERSION 1
+
+enum {
+  NBFMM_OK = 0,
+  NBFMM_ERR_INVALID = 1, /* an argument the reference asserts on (solver.cu:24-27, solve.cu:17, stars.cu:36-43) */
+  NBFMM_ERR_CUDA = 2,    /* a CUDA runtime error; the message names the call */
+  NBFMM_ERR_NOMEM = 3    /* device memory could not be allocated */
+};
+
+typedef struct nbfmm_solver nbfmm_solver;
+typedef struct nbfmm_stars nbfmm_stars;
+
+/* Message of the last failed call on this host thread ("" when none). */
+const char* nbfmm_last_error(void);
+int nbfmm_version(void);
+
+/* ---- Solver ---------------------------------------------------------------------------------------- */
+
+/* nbfmm::Solver::Solver(num_level, max_num_particle, position_limits)  (solver.hpp:80-89, solver.cu:14-46).
+ * 0 <= num_level <= 10 (base_dim = 2^(num_level+1)), 1 <= max_num_particle <= 2^28, limits ordered.
+ * Allocates the whole workspace; no later call allocates device memory. */
+int nbfmm_solver_create(int num_level, int max_num_particle, const float position_limits[4], nbfmm_solver** out);
+
+/* nbfmm::Solver::~Solver  (solver.cu:49-61). NULL is accepted. */
+int nbfmm_solver_destroy(nbfmm_solver* solver);
+
+/* Softening of the kernel a = d*m/(|d|^3 + eps); the reference fixes eps = 1e-1
+ * (include/nbfmm/core/kernel_function.hpp:35), which is the default here. */
+int nbfmm_solver_set_epsilon(nbfmm_solver* solver, float epsilon);
+
+/* nbfmm::Solver::solve(num_particle, position, weight, effect)  (solver.hpp:91-103, solve.cu:11-27).
+ * Positions/weights in the caller's order in, effects in the caller's order out; 0 <= n <= max. */
+int nbfmm_solver_solve(nbfmm_solver* solver, int num_particle, const float* gpuptr_position_origin,
+                       const float* gpuptr_weight_origin, float* gpuptr_effect_origin, void* stream);
+
+/* The stage methods, public in the reference under NBFMM_CHECK (solver.hpp:24-28, 105-209). They run on
+ * the solver's own buffers (nbfmm_solver_get_buffers), exactly as the reference's tests drive them. */
+int nbfmm_solver_predo(nbfmm_solver* solver, int num_particle, const float* gpuptr_position_origin,
+                       const float* gpuptr_weight_origin, void* stream);         /* predo.cu:105-135 */
+int nbfmm_solver_p2p(nbfmm_solver* solver, int num_particle, void* stream);     /* p2p.cu:165-176 */
+int nbfmm_solver_p2m(nbfmm_solver* solver, int num_particle, void* stream);     /* p2m.cu:79-110 */
+int nbfmm_solver_m2m(nbfmm_solver* solver, void* stream);                       /* m2m.cu:58-74 */
+int nbfmm_solver_m2l(nbfmm_solver* solver, void* stream);                       /* m2l.cu:63-81 */
+int nbfmm_solver_l2l(nbfmm_solver* solver, void* stream);                       /* l2l.cu:39-56 */
+int nbfmm_solver_l2p(nbfmm_solver* solver, int num_particle, void* stream);     /* l2p.cu:38-48 */
+int nbfmm_solver_postdo(nbfmm_solver* solver, int num_particle, float* gpuptr_effect_origin,
+                        void* stream);                                          /* postdo.cu:36-45 */
+
+/* The workspace, the reference's gpuptr_* members (solver.hpp:42-79) in this engine's layout:
+ *   particle     float4 [max_num_particle]  sorted x, y, weight, original index (int bits)
+ *                                           (gpuptr_position_ + gpuptr_weight_ + gpuptr_perm_)
+ *   effect       float2 [max_num_particle]  sorted effects (gpuptr_effect_)
+ *   cell_key     uint32 [max_num_particle]  sorted leaf key ix + iy*base_dim (gpuptr_index_)
+ *   perm         uint32 [max_num_particle]  sorted -> original index (gpuptr_perm_)
+ *   head         int32  [base_dim^2 + 1]    (gpuptr_head_)
+ *   cell         float4 [total_cells]       centre of mass x, y, mass, 0 (gpuptr_cell_position_/_weight_)
+ *   cell_effect  float2 [total_cells]       (gpuptr_cell_effect_)
+ * Cell level l holds level_dim[l]^2 cells, row-major, starting at cell level_offset[l]
+ * (the reference's strided cube keeps cell (x,y) of level l at l*B*B + (x + y*B) << l). */
+typedef struct {
+  int num_level;
+  int base_dim;
+  int max_num_particle;
+  int num_cell_levels;
+  int level_dim[11];
+  int level_offset[11];
+  int total_cells;
+  float* particle;
+  float* effect;
+  unsigned int* cell_key;
+  unsigned int* perm;
+  int* head;
+  float* cell;
+  float* cell_effect;
+} nbfmm_solver_buffers;
+
+int nbfmm_solver_get_buffers(nbfmm_solver* solver, nbfmm_solver_buffers* out);
+
+/* ---- Stars (the update path) ----------------------------------------------------------------------- */
+
+/* nbfmm::Stars::Stars(fmm_level, num_star, ..., tick, grav_const, ..., position_limits, ...)
+ * (stars.hpp:90-98, stars.cu:15-50). The display-only arguments (width, height, fps, size_scale,
+ * display_limits) are not part of this path. The effective tick is tick * sqrt(grav_const) (stars.cu:31). */
+int nbfmm_stars_create(int fmm_level, int num_star, float tick, float grav_const, const float position_limits[4],
+                       nbfmm_stars** out);
+int nbfmm_stars_destroy(nbfmm_stars* stars);
+int nbfmm_stars_set_epsilon(nbfmm_stars* stars, float epsilon);
+
+/* The public state members (stars.hpp:60-72): gpuptr_position_cur_, gpuptr_position_pre_ (float2 [num_star]),
+ * gpuptr_weight_ (float [num_star]). Stars::initialize (stars.hpp:111-114) is the caller writing these. */
+int nbfmm_stars_state(nbfmm_stars* stars, float** gpuptr_position_cur, float** gpuptr_position_pre,
+                      float** gpuptr_weight);
+
+/* Current number of stars (num_star_, stars.hpp:34). Synchronises with the last update's stream. */
+int nbfmm_stars_num_star(nbfmm_stars* stars, int* num_star);
+
+/* num_steps calls of nbfmm::Stars::update() (update.cu:47-55): solve, Stormer-Verlet update, prune.
+ * After the call the state arrays hold the surviving stars first, in their previous relative order,
+ * followed by the pruned ones, most recently pruned first, as num_steps reference updates leave them.
+ * Runs without host synchronisation; the steps are replayed from a captured CUDA graph. */
+int nbfmm_stars_update(nbfmm_stars* stars, int num_steps, void* stream);
+
+/* ---- Instrumentation (engine-only; the reference has no timing, no events, no counters) ------------ */
+
+/* Times the P2P launch of each of the next `max_steps` update steps with a pair of CUDA events recorded
+ * on the update's stream around that launch (the event record nodes of the captured step graph are
+ * pointed at a fresh pair per step). */
+int nbfmm_stars_profile_begin(nbfmm_stars* stars, int max_steps);
+
+/* Ends the session: total P2P milliseconds and number of timed launches. Synchronises. */
+int nbfmm_stars_profile_end(nbfmm_stars* stars, float* p2p_ms_total, int* p2p_launches);
+
+/* Number of engine kernels one nbfmm_stars_update(stars, num_steps) call launches. */
+int nbfmm_stars_kernel_launches(nbfmm_stars* stars, int num_steps, long long* launches);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* NBFMM_GB300_H_ */

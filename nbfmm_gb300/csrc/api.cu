@@ -1,0 +1,677 @@
+// api.cu -- C ABI of the GB300 engine (include/nbfmm_gb300.h): workspace, stage sequencing, the fused
+// solve path and the graph-replayed Stars update.
+//
+// Solve path (solve.cu:11-27 of the reference, reordered so that the far field is ready before P2P and the
+// L2P + postdo work rides in the P2P epilogue):
+//   keys -> stable radix sort -> head + work list -> gather + P2M -> M2M -> M2L+L2L -> P2P(+L2P+postdo)
+// No call allocates device memory after create, and no call synchronises the host except
+// nbfmm_stars_num_star and the first nbfmm_stars_update of a handle (graph instantiation).
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "../../include/nbfmm_gb300.h"
+#include "engine.cuh"
+#include "stars.cuh"
+
+using namespace nbfmm_gb300;
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int fail(int code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  std::vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  g_last_error = buf;
+  return code;
+}
+
+int cuda_check(const char* what) {
+  const cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return fail(NBFMM_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+  return NBFMM_OK;
+}
+
+#define NBFMM_TRY(expr)              \
+  do {                               \
+    const int _rc = (expr);          \
+    if (_rc != NBFMM_OK) return _rc; \
+  } while (0)
+
+template <typename T>
+int dalloc(T** p, size_t count, const char* what) {
+  *p = nullptr;
+  if (count == 0) count = 1;
+  const cudaError_t e = cudaMalloc(reinterpret_cast<void**>(p), count * sizeof(T));
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    *p = nullptr;
+    return fail(e == cudaErrorMemoryAllocation ? NBFMM_ERR_NOMEM : NBFMM_ERR_CUDA, "cudaMalloc(%s, %zu bytes): %s",
+                what, count * sizeof(T), cudaGetErrorString(e));
+  }
+  return NBFMM_OK;
+}
+
+template <typename T>
+void dfree(T*& p) {
+  if (p) cudaFree(p);
+  p = nullptr;
+}
+
+bool limits_ok(const float* l) {
+  return l && std::isfinite(l[0]) && std::isfinite(l[1]) && std::isfinite(l[2]) && std::isfinite(l[3]) &&
+         l[0] < l[2] && l[1] < l[3];
+}
+
+}  // namespace
+
+// ---- Solver --------------------------------------------------------------------------------------------
+
+struct nbfmm_solver {
+  Geometry geo{};
+  Levels lv{};
+  int max_n = 0;
+  int num_cells = 0;   // B*B
+  int key_bits = 0;    // bits of the largest key the sort sees
+  int max_tiles = 0;
+  int num_sms = 0;
+  float eps = 0.1f;
+
+  uint32_t *keys_a = nullptr, *vals_a = nullptr, *keys_b = nullptr, *vals_b = nullptr;
+  uint32_t *counts = nullptr, *digit_total = nullptr;
+  int* head = nullptr;
+  int2* work = nullptr;
+  float4* sorted4 = nullptr;
+  float2* seff = nullptr;
+  float4* cell4 = nullptr;
+  float2* ceff = nullptr;
+  int* ints = nullptr;  // [0] n, [1] n_alive, [2] work count, [3] work counter
+  // Where the last sort left its result.
+  uint32_t* skey = nullptr;
+  uint32_t* perm = nullptr;
+
+  int* d_n() { return ints + 0; }
+  int* d_n_alive() { return ints + 1; }
+  int* d_work_count() { return ints + 2; }
+  int* d_work_next() { return ints + 3; }
+
+  int init(int num_level, int max_num_particle, const float* limits, int extra_key_bits) {
+    const int B = 1 << (num_level + 1);
+    geo.xmin = limits[0];
+    geo.ymin = limits[1];
+    geo.xmax = limits[2];
+    geo.ymax = limits[3];
+    geo.cell_x = (limits[2] - limits[0]) / (float)B;  // predo.cu:112-113
+    geo.cell_y = (limits[3] - limits[1]) / (float)B;
+    geo.num_level = num_level;
+    geo.base_dim = B;
+    lv.count = num_level > 0 ? num_level : 1;
+    lv.total = 0;
+    for (int l = 0; l < lv.count; ++l) {
+      lv.dim[l] = B >> l;
+      lv.offset[l] = lv.total;
+      lv.total += lv.dim[l] * lv.dim[l];
+    }
+    max_n = max_num_particle;
+    num_cells = B * B;
+    key_bits = 2 * (num_level + 1) + extra_key_bits;
+    max_tiles = (max_n + kSortTile - 1) / kSortTile;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&num_sms, cudaDevAttrMultiProcessorCount, dev);
+    NBFMM_TRY(cuda_check("device query"));
+    const size_t n = (size_t)max_n;
+    NBFMM_TRY(dalloc(&keys_a, n, "keys"));
+    NBFMM_TRY(dalloc(&vals_a, n, "values"));
+    NBFMM_TRY(dalloc(&keys_b, n, "keys"));
+    NBFMM_TRY(dalloc(&vals_b, n, "values"));
+    NBFMM_TRY(dalloc(&counts, (size_t)(1 << kRadixMaxBits) * max_tiles, "tile counts"));
+    NBFMM_TRY(dalloc(&digit_total, (size_t)(1 << kRadixMaxBits), "digit totals"));
+    NBFMM_TRY(dalloc(&head, (size_t)num_cells + 2, "head"));
+    NBFMM_TRY(dalloc(&work, (size_t)num_cells + n / kP2PChunk + 1, "work list"));
+    NBFMM_TRY(dalloc(&sorted4, n, "sorted particles"));
+    NBFMM_TRY(dalloc(&seff, n, "sorted effects"));
+    NBFMM_TRY(dalloc(&cell4, (size_t)lv.total, "cells"));
+    NBFMM_TRY(dalloc(&ceff, (size_t)lv.total, "cell effects"));
+    NBFMM_TRY(dalloc(&ints, 8, "counters"));
+    cudaMemset(ints, 0, 8 * sizeof(int));
+    cudaMemset(head, 0, ((size_t)num_cells + 2) * sizeof(int));
+    cudaMemset(cell4, 0, (size_t)lv.total * sizeof(float4));
+    cudaMemset(ceff, 0, (size_t)lv.total * sizeof(float2));
+    NBFMM_TRY(cuda_check("workspace clear"));
+    skey = keys_a;
+    perm = vals_a;
+    return NBFMM_OK;
+  }
+
+  ~nbfmm_solver() {
+    dfree(keys_a); dfree(vals_a); dfree(keys_b); dfree(vals_b);
+    dfree(counts); dfree(digit_total); dfree(head); dfree(work);
+    dfree(sorted4); dfree(seff); dfree(cell4); dfree(ceff); dfree(ints);
+  }
+
+  float4* cell0() { return cell4 + lv.offset[0]; }
+  float2* ceff0() { return ceff + lv.offset[0]; }
+
+  // Sort (keys_a, vals_a) holding d_n entries; records where the result went.
+  void sort(const int* dn, int bits, cudaStream_t s) {
+    const int where = launch_radix_sort(keys_a, vals_a, keys_b, vals_b, counts, digit_total, dn, max_n, bits, s);
+    skey = where ? keys_b : keys_a;
+    perm = where ? vals_b : vals_a;
+  }
+
+  // Keys, sort, head and work list from caller-order positions (predo.cu:105-135 minus the gather).
+  void preassign(int n, const float2* pos, cudaStream_t s) {
+    launch_set_int(d_n(), n, s);
+    launch_keys_from_positions(geo, pos, d_n(), keys_a, vals_a, max_n, s);
+    sort(d_n(), key_bits, s);
+    launch_head(skey, d_n(), num_cells, head, d_n_alive(), s);
+    launch_worklist(head, num_cells, work, d_work_count(), s);
+  }
+
+  void far_field(cudaStream_t s) {
+    if (geo.num_level <= 0) return;  // p2m.cu:80, m2l.cu:64
+    launch_m2m(lv, cell4, s);         // no-op for num_level <= 1 (m2m.cu:60)
+    launch_m2l(lv, cell4, ceff, eps, true, s);
+  }
+
+  P2PArgs p2p_args() {
+    P2PArgs a{};
+    a.sorted4 = sorted4;
+    a.head = head;
+    a.work = work;
+    a.d_work_count = d_work_count();
+    a.d_work_next = d_work_next();
+    a.base_dim = geo.base_dim;
+    a.eps = eps;
+    a.ceff0 = geo.num_level > 0 ? ceff0() : nullptr;
+    return a;
+  }
+
+  int solve(int n, const float* pos, const float* w, float* eff, cudaStream_t s) {
+    if (n == 0) return NBFMM_OK;
+    preassign(n, reinterpret_cast<const float2*>(pos), s);
+    launch_gather_p2m(geo, head, perm, reinterpret_cast<const float2*>(pos), w, sorted4, cell0(), s);
+    far_field(s);
+    P2PArgs a = p2p_args();
+    a.eff_origin = reinterpret_cast<float2*>(eff);
+    launch_p2p(a, kSolve, num_sms, s);
+    return cuda_check("nbfmm_solver_solve");
+  }
+};
+
+namespace {
+
+int check_solver(nbfmm_solver* h) { return h ? NBFMM_OK : fail(NBFMM_ERR_INVALID, "null solver handle"); }
+
+int check_n(nbfmm_solver* h, int n) {
+  if (n < 0 || n > h->max_n) {
+    return fail(NBFMM_ERR_INVALID, "num_particle %d outside [0, %d] (solve.cu:17)", n, h->max_n);
+  }
+  return NBFMM_OK;
+}
+
+int make_solver(int num_level, int max_num_particle, const float* limits, int extra_key_bits, nbfmm_solver** out) {
+  if (!out) return fail(NBFMM_ERR_INVALID, "null output pointer");
+  *out = nullptr;
+  if (num_level < 0 || num_level > kMaxLevels - 1) {
+    return fail(NBFMM_ERR_INVALID, "num_level %d outside [0, %d]", num_level, kMaxLevels - 1);
+  }
+  if (max_num_particle < 1 || max_num_particle > (1 << 28)) {
+    return fail(NBFMM_ERR_INVALID, "max_num_particle %d outside [1, 2^28]", max_num_particle);
+  }
+  if (!limits_ok(limits)) return fail(NBFMM_ERR_INVALID, "position limits must be finite with min < max");
+  nbfmm_solver* h = new (std::nothrow) nbfmm_solver();
+  if (!h) return fail(NBFMM_ERR_NOMEM, "host allocation failed");
+  const int rc = h->init(num_level, max_num_particle, limits, extra_key_bits);
+  if (rc != NBFMM_OK) {
+    delete h;
+    return rc;
+  }
+  *out = h;
+  return NBFMM_OK;
+}
+
+cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s); }
+
+}  // namespace
+
+extern "C" {
+
+const char* nbfmm_last_error(void) { return g_last_error.c_str(); }
+
+int nbfmm_version(void) { return NBFMM_GB300_VERSION; }
+
+int nbfmm_solver_create(int num_level, int max_num_particle, const float position_limits[4], nbfmm_solver** out) {
+  return make_solver(num_level, max_num_particle, position_limits, 0, out);
+}
+
+int nbfmm_solver_destroy(nbfmm_solver* solver) {
+  delete solver;
+  return NBFMM_OK;
+}
+
+int nbfmm_solver_set_epsilon(nbfmm_solver* solver, float epsilon) {
+  NBFMM_TRY(check_solver(solver));
+  if (!(epsilon > 0.0f) || !std::isfinite(epsilon)) return fail(NBFMM_ERR_INVALID, "epsilon must be finite and > 0");
+  solver->eps = epsilon;
+  return NBFMM_OK;
+}
+
+int nbfmm_solver_solve(nbfmm_solver* solver, int num_particle, const float* gpuptr_position_origin,
+                       const float* gpuptr_weight_origin, float* gpuptr_effect_origin, void* stream) {
+  NBFMM_TRY(check_solver(solver));
+  NBFMM_TRY(check_n(solver, num_particle));
+  if (num_particle > 0 && (!gpuptr_position_origin || !gpuptr_weight_origin || !gpuptr_effect_origin)) {
+    return fail(NBFMM_ERR_INVALID, "null device pointer");
+  }
+  return solver->solve(num_particle, gpuptr_position_origin, gpuptr_weight_origin, gpuptr_effect_origin,
+                       as_stream(stream));
+}
+
+int nbfmm_solver_predo(nbfmm_solver* solver, int num_particle, const float* gpuptr_position_origin,
+                       const float* gpuptr_weight_origin, void* stream) {
+  NBFMM_TRY(check_solver(solver));
+  NBFMM_TRY(check_n(solver, num_particle));
+  if (num_particle > 0 && (!gpuptr_position_origin || !gpuptr_weight_origin)) {
+    return fail(NBFMM_ERR_INVALID, "null device pointer");
+  }
+  cudaStream_t s = as_stream(stream);
+  solver->preassign(num_particle, reinterpret_cast<const float2*>(gpuptr_position_origin), s);
+  launch_gather_p2m(solver->geo, solver->head, solver->perm, reinterpret_cast<const float2*>(gpuptr_position_origin),
+                    gpuptr_weight_origin, solver->sorted4, solver->cell0(), s);
+  return cuda_check("nbfmm_solver_predo");
+}
+
+int nbfmm_solver_p2p(nbfmm_solver* solver, int num_particle, void* stream) {
+  NBFMM_TRY(check_solver(solver));
+  NBFMM_TRY(check_n(solver, num_particle));
+  cudaStream_t s = as_stream(stream);
+  launch_worklist(solver->head, solver->num_cells, solver->work, solver->d_work_count(), s);
+  P2PArgs a = solver->p2p_args();
+  a.seff = solver->seff;
+  launch_p2p(a, kStoreSorted, solver->num_sms, s);
+  return cuda_check("nbfmm_solver_p2p");
+}
+
+int nbfmm_solver_p2m(nbfmm_solver* solver, int num_particle, void* stream) {
+  NBFMM_TRY(check_solver(solver));
+  NBFMM_TRY(check_n(solver, num_particle));
+  if (solver->geo.num_level <= 0) return NBFMM_OK;  // p2m.cu:80
+  launch_p2m(solver->geo, solver->head, solver->sorted4, solver->cell0(), as_stream(stream));
+  return cuda_check("nbfmm_solver_p2m");
+}
+
+int nbfmm_solver_m2m(nbfmm_solver* solver, void* stream) {
+  NBFMM_TRY(check_solver(solver));
+  if (solver->geo.num_level <= 1) return NBFMM_OK;  // m2m.cu:60
+  launch_m2m(solver->lv, solver->cell4, as_stream(stream));
+  return cuda_check("nbfmm_solver_m2m");
+}
+
+int nbfmm_solver_m2l(nbfmm_solver* solver, void* stream) {
+  NBFMM_TRY(check_solver(solver));
+  if (solver->geo.num_level <= 0) return NBFMM_OK;  // m2l.cu:64
+  launch_m2l(solver->lv, solver->cell4, solver->ceff, solver->eps, false, as_stream(stream));
+  return cuda_check("nbfmm_solver_m2l");
+}
+
+int nbfmm_solver_l2l(nbfmm_solver* solver, void* stream) {
+  NBFMM_TRY(check_solver(solver));
+  if (solver->geo.num_level <= 1) return NBFMM_OK;  // l2l.cu:40
+  launch_l2l(solver->lv, solver->ceff, as_stream(stream));
+  return cuda_check("nbfmm_solver_l2l");
+}
+
+int nbfmm_solver_l2p(nbfmm_solver* solver, int num_particle, void* stream) {
+  NBFMM_TRY(check_solver(solver));
+  NBFMM_TRY(check_n(solver, num_particle));
+  if (solver->geo.num_level <= 0) return NBFMM_OK;  // l2p.cu:39
+  cudaStream_t s = as_stream(stream);
+  launch_set_int(solver->d_n(), num_particle, s);
+  launch_l2p(solver->d_n(), solver->skey, solver->ceff0(), solver->seff, solver->max_n, s);
+  return cuda_check("nbfmm_solver_l2p");
+}
+
+int nbfmm_solver_postdo(nbfmm_solver* solver, int num_particle, float* gpuptr_effect_origin, void* stream) {
+  NBFMM_TRY(check_solver(solver));
+  NBFMM_TRY(check_n(solver, num_particle));
+  if (num_particle > 0 && !gpuptr_effect_origin) return fail(NBFMM_ERR_INVALID, "null device pointer");
+  cudaStream_t s = as_stream(stream);
+  launch_set_int(solver->d_n(), num_particle, s);
+  launch_postdo(solver->d_n(), solver->perm, solver->seff, reinterpret_cast<float2*>(gpuptr_effect_origin),
+                solver->max_n, s);
+  return cuda_check("nbfmm_solver_postdo");
+}
+
+int nbfmm_solver_get_buffers(nbfmm_solver* solver, nbfmm_solver_buffers* out) {
+  NBFMM_TRY(check_solver(solver));
+  if (!out) return fail(NBFMM_ERR_INVALID, "null output pointer");
+  std::memset(out, 0, sizeof(*out));
+  out->num_level = solver->geo.num_level;
+  out->base_dim = solver->geo.base_dim;
+  out->max_num_particle = solver->max_n;
+  out->num_cell_levels = solver->lv.count;
+  for (int l = 0; l < solver->lv.count; ++l) {
+    out->level_dim[l] = solver->lv.dim[l];
+    out->level_offset[l] = solver->lv.offset[l];
+  }
+  out->total_cells = solver->lv.total;
+  out->particle = reinterpret_cast<float*>(solver->sorted4);
+  out->effect = reinterpret_cast<float*>(solver->seff);
+  out->cell_key = solver->skey;
+  out->perm = solver->perm;
+  out->head = solver->head;
+  out->cell = reinterpret_cast<float*>(solver->cell4);
+  out->cell_effect = reinterpret_cast<float*>(solver->ceff);
+  return NBFMM_OK;
+}
+
+}  // extern "C"
+
+// ---- Stars ---------------------------------------------------------------------------------------------
+
+struct nbfmm_stars {
+  nbfmm_solver* solver = nullptr;
+  int max_n = 0;
+  float tick = 0.0f;  // tick * sqrt(grav_const), stars.cu:31
+  // Public state, the reference's layout (stars.hpp:60-72).
+  float2* cur = nullptr;
+  float2* prev = nullptr;
+  float* w = nullptr;
+  // Internal state and files by original index.
+  float4* state4 = nullptr;
+  float2* state_prev = nullptr;
+  float2* sprev = nullptr;
+  float2* grave_cur = nullptr;
+  float2* grave_prev = nullptr;
+  float* w_by_orig = nullptr;
+  int* fate = nullptr;
+  int* counters = nullptr;
+  StepCounters sc{};
+  cudaStream_t capture_stream = nullptr;
+  cudaGraph_t step_graph_def = nullptr;
+  cudaGraphExec_t step_graph = nullptr;
+  // Event record nodes around P2P in the step graph, and the profiling session's events.
+  cudaEvent_t cap_a = nullptr, cap_b = nullptr;
+  cudaGraphNode_t node_a = nullptr, node_b = nullptr;
+  int kernels_per_step = 0;
+  std::vector<cudaEvent_t> prof_events;
+  int prof_max = 0, prof_used = 0;
+
+  int init(int fmm_level, int num_star, float tick_scaled, const float* limits) {
+    NBFMM_TRY(make_solver(fmm_level, num_star > 0 ? num_star : 1, limits, 1, &solver));
+    max_n = num_star > 0 ? num_star : 1;
+    tick = tick_scaled;
+    const size_t n = (size_t)max_n;
+    NBFMM_TRY(dalloc(&cur, n, "position_cur"));
+    NBFMM_TRY(dalloc(&prev, n, "position_pre"));
+    NBFMM_TRY(dalloc(&w, n, "weight"));
+    NBFMM_TRY(dalloc(&state4, n, "state"));
+    NBFMM_TRY(dalloc(&state_prev, n, "state prev"));
+    NBFMM_TRY(dalloc(&sprev, n, "sorted prev"));
+    NBFMM_TRY(dalloc(&grave_cur, n, "final positions"));
+    NBFMM_TRY(dalloc(&grave_prev, n, "final previous positions"));
+    NBFMM_TRY(dalloc(&w_by_orig, n, "weights by index"));
+    NBFMM_TRY(dalloc(&fate, n, "fates"));
+    NBFMM_TRY(dalloc(&counters, 8, "step counters"));
+    cudaMemset(cur, 0, n * sizeof(float2));
+    cudaMemset(prev, 0, n * sizeof(float2));
+    cudaMemset(w, 0, n * sizeof(float));
+    cudaMemset(counters, 0, 8 * sizeof(int));
+    sc.num_star = counters + 0;
+    sc.n_import = counters + 1;
+    sc.n_cur = counters + 2;
+    sc.n_alive = solver->d_n_alive();
+    sc.step = counters + 3;
+    sc.prune = counters + 4;
+    sc.num_steps = counters + 5;
+    launch_set_int(sc.num_star, num_star, nullptr);
+    if (cudaStreamCreateWithFlags(&capture_stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreate(&cap_a) != cudaSuccess || cudaEventCreate(&cap_b) != cudaSuccess) {
+      return cuda_check("stream/event create");
+    }
+    NBFMM_TRY(cuda_check("stars init"));
+    return cudaDeviceSynchronize() == cudaSuccess ? NBFMM_OK : cuda_check("stars init sync");
+  }
+
+  void drop_graph() {
+    if (step_graph) cudaGraphExecDestroy(step_graph);
+    if (step_graph_def) cudaGraphDestroy(step_graph_def);
+    step_graph = nullptr;
+    step_graph_def = nullptr;
+    node_a = node_b = nullptr;
+  }
+
+  void drop_profile_events() {
+    for (cudaEvent_t e : prof_events) cudaEventDestroy(e);
+    prof_events.clear();
+    prof_max = prof_used = 0;
+  }
+
+  ~nbfmm_stars() {
+    drop_graph();
+    drop_profile_events();
+    if (cap_a) cudaEventDestroy(cap_a);
+    if (cap_b) cudaEventDestroy(cap_b);
+    if (capture_stream) cudaStreamDestroy(capture_stream);
+    dfree(cur); dfree(prev); dfree(w); dfree(state4); dfree(state_prev); dfree(sprev);
+    dfree(grave_cur); dfree(grave_prev); dfree(w_by_orig); dfree(fate); dfree(counters);
+    delete solver;
+  }
+
+  // One step: keys (with the prune of the previous step), sort, head, gather + P2M, far field,
+  // P2P + L2P + Verlet into the state, counters.
+  void enqueue_step(cudaStream_t s) {
+    nbfmm_solver& v = *solver;
+    const uint32_t dead = (uint32_t)v.num_cells;
+    launch_keys_from_state(v.geo, sc, state4, state_prev, dead, v.keys_a, v.vals_a, grave_cur, grave_prev, fate,
+                           max_n, s);
+    v.sort(sc.n_cur, v.key_bits, s);
+    launch_head(v.skey, sc.n_cur, v.num_cells, v.head, sc.n_alive, s);
+    launch_worklist(v.head, v.num_cells, v.work, v.d_work_count(), s);
+    launch_gather_state_p2m(v.geo, v.head, v.perm, state4, state_prev, v.sorted4, sprev, v.cell0(), s);
+    v.far_field(s);
+    P2PArgs a = v.p2p_args();
+    a.sprev = sprev;
+    a.state4 = state4;
+    a.state_prev = state_prev;
+    a.tick = tick;
+    cudaEventRecord(cap_a, s);
+    launch_p2p(a, kVerlet, v.num_sms, s);
+    cudaEventRecord(cap_b, s);
+    launch_finish_step(sc, s);
+  }
+
+  int build_graph() {
+    cudaGraph_t g = nullptr;
+    if (cudaStreamBeginCapture(capture_stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+      return cuda_check("cudaStreamBeginCapture");
+    }
+    enqueue_step(capture_stream);
+    const cudaError_t e = cudaStreamEndCapture(capture_stream, &g);
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      return fail(NBFMM_ERR_CUDA, "step capture: %s", cudaGetErrorString(e));
+    }
+    const cudaError_t e2 = cudaGraphInstantiate(&step_graph, g, 0);
+    if (e2 != cudaSuccess) {
+      cudaGetLastError();
+      cudaGraphDestroy(g);
+      step_graph = nullptr;
+      return fail(NBFMM_ERR_CUDA, "step graph instantiate: %s", cudaGetErrorString(e2));
+    }
+    step_graph_def = g;
+    size_t count = 0;
+    cudaGraphGetNodes(g, nullptr, &count);
+    std::vector<cudaGraphNode_t> nodes(count);
+    cudaGraphGetNodes(g, nodes.data(), &count);
+    kernels_per_step = 0;
+    for (cudaGraphNode_t nd : nodes) {
+      cudaGraphNodeType type;
+      cudaGraphNodeGetType(nd, &type);
+      if (type == cudaGraphNodeTypeKernel) ++kernels_per_step;
+      if (type == cudaGraphNodeTypeEventRecord) {
+        cudaEvent_t ev = nullptr;
+        cudaGraphEventRecordNodeGetEvent(nd, &ev);
+        if (ev == cap_a) node_a = nd;
+        if (ev == cap_b) node_b = nd;
+      }
+    }
+    if (!node_a || !node_b) return fail(NBFMM_ERR_CUDA, "step graph: P2P event nodes not found");
+    return cuda_check("step graph inspection");
+  }
+
+  // Kernels outside the step graph per update call: import, step count, and the final prune/reorder.
+  int sort_passes(int bits) const { return (bits + kRadixMaxBits - 1) / kRadixMaxBits; }
+  static int fate_bits(int steps) {
+    int bits = 1;
+    while ((1 << bits) <= steps + 1) ++bits;
+    return bits;
+  }
+
+  int update(int steps, cudaStream_t s) {
+    if (steps <= 0) return NBFMM_OK;
+    if (!step_graph) NBFMM_TRY(build_graph());
+    nbfmm_solver& v = *solver;
+    launch_import(sc, cur, prev, w, state4, state_prev, w_by_orig, max_n, s);
+    launch_set_int(sc.num_steps, steps, s);
+    for (int k = 0; k < steps; ++k) {
+      if (prof_used < prof_max) {  // point the P2P event nodes at this step's pair
+        cudaGraphExecEventRecordNodeSetEvent(step_graph, node_a, prof_events[2 * prof_used]);
+        cudaGraphExecEventRecordNodeSetEvent(step_graph, node_b, prof_events[2 * prof_used + 1]);
+        ++prof_used;
+      } else if (prof_max > 0 && prof_used == prof_max) {
+        cudaGraphExecEventRecordNodeSetEvent(step_graph, node_a, cap_a);
+        cudaGraphExecEventRecordNodeSetEvent(step_graph, node_b, cap_b);
+        ++prof_used;
+      }
+      if (cudaGraphLaunch(step_graph, s) != cudaSuccess) return cuda_check("cudaGraphLaunch");
+    }
+    // Final prune and the reference's order: survivors (fate 0) in original order, then the pruned stars,
+    // most recent first (fate 1, 2, ...), each group in original order.
+    launch_export_fate(v.geo, sc, state4, state_prev, grave_cur, grave_prev, fate, max_n, s);
+    launch_fate_keys(sc, fate, v.keys_a, v.vals_a, max_n, s);
+    v.sort(sc.n_import, fate_bits(steps), s);
+    launch_head(v.skey, sc.n_import, 1, v.head, sc.num_star, s);  // head[1] = number of fate-0 stars
+    launch_export_gather(sc, v.perm, grave_cur, grave_prev, w_by_orig, cur, prev, w, max_n, s);
+    return cuda_check("nbfmm_stars_update");
+  }
+};
+
+extern "C" {
+
+int nbfmm_stars_create(int fmm_level, int num_star, float tick, float grav_const, const float position_limits[4],
+                       nbfmm_stars** out) {
+  if (!out) return fail(NBFMM_ERR_INVALID, "null output pointer");
+  *out = nullptr;
+  if (num_star < 0) return fail(NBFMM_ERR_INVALID, "num_star must be >= 0 (stars.cu:36)");
+  const float tick_scaled = tick * std::sqrt(grav_const);  // stars.cu:31
+  if (!(tick_scaled > 0.0f) || !std::isfinite(tick_scaled)) {
+    return fail(NBFMM_ERR_INVALID, "tick * sqrt(grav_const) must be finite and > 0 (stars.cu:40)");
+  }
+  nbfmm_stars* h = new (std::nothrow) nbfmm_stars();
+  if (!h) return fail(NBFMM_ERR_NOMEM, "host allocation failed");
+  const int rc = h->init(fmm_level, num_star, tick_scaled, position_limits);
+  if (rc != NBFMM_OK) {
+    delete h;
+    return rc;
+  }
+  *out = h;
+  return NBFMM_OK;
+}
+
+int nbfmm_stars_destroy(nbfmm_stars* stars) {
+  delete stars;
+  return NBFMM_OK;
+}
+
+int nbfmm_stars_set_epsilon(nbfmm_stars* stars, float epsilon) {
+  if (!stars) return fail(NBFMM_ERR_INVALID, "null stars handle");
+  stars->drop_graph();  // the graph captured the old value
+  return nbfmm_solver_set_epsilon(stars->solver, epsilon);
+}
+
+int nbfmm_stars_state(nbfmm_stars* stars, float** gpuptr_position_cur, float** gpuptr_position_pre,
+                      float** gpuptr_weight) {
+  if (!stars) return fail(NBFMM_ERR_INVALID, "null stars handle");
+  if (gpuptr_position_cur) *gpuptr_position_cur = reinterpret_cast<float*>(stars->cur);
+  if (gpuptr_position_pre) *gpuptr_position_pre = reinterpret_cast<float*>(stars->prev);
+  if (gpuptr_weight) *gpuptr_weight = stars->w;
+  return NBFMM_OK;
+}
+
+int nbfmm_stars_num_star(nbfmm_stars* stars, int* num_star) {
+  if (!stars || !num_star) return fail(NBFMM_ERR_INVALID, "null argument");
+  if (cudaMemcpy(num_star, stars->sc.num_star, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess) {
+    return cuda_check("nbfmm_stars_num_star");
+  }
+  return NBFMM_OK;
+}
+
+int nbfmm_stars_update(nbfmm_stars* stars, int num_steps, void* stream) {
+  if (!stars) return fail(NBFMM_ERR_INVALID, "null stars handle");
+  if (num_steps < 0) return fail(NBFMM_ERR_INVALID, "num_steps must be >= 0");
+  return stars->update(num_steps, as_stream(stream));
+}
+
+int nbfmm_stars_profile_begin(nbfmm_stars* stars, int max_steps) {
+  if (!stars) return fail(NBFMM_ERR_INVALID, "null stars handle");
+  if (max_steps < 0) return fail(NBFMM_ERR_INVALID, "max_steps must be >= 0");
+  if (!stars->step_graph) NBFMM_TRY(stars->build_graph());
+  stars->drop_profile_events();
+  stars->prof_events.resize(2 * (size_t)max_steps, nullptr);
+  for (auto& e : stars->prof_events) {
+    if (cudaEventCreate(&e) != cudaSuccess) return cuda_check("cudaEventCreate");
+  }
+  stars->prof_max = max_steps;
+  stars->prof_used = 0;
+  return NBFMM_OK;
+}
+
+int nbfmm_stars_profile_end(nbfmm_stars* stars, float* p2p_ms_total, int* p2p_launches) {
+  if (!stars || !p2p_ms_total || !p2p_launches) return fail(NBFMM_ERR_INVALID, "null argument");
+  const int used = stars->prof_used < stars->prof_max ? stars->prof_used : stars->prof_max;
+  float total = 0.0f;
+  for (int k = 0; k < used; ++k) {
+    if (cudaEventSynchronize(stars->prof_events[2 * k + 1]) != cudaSuccess) return cuda_check("cudaEventSynchronize");
+    float ms = 0.0f;
+    if (cudaEventElapsedTime(&ms, stars->prof_events[2 * k], stars->prof_events[2 * k + 1]) != cudaSuccess) {
+      return cuda_check("cudaEventElapsedTime");
+    }
+    total += ms;
+  }
+  if (stars->step_graph && stars->node_a) {
+    cudaGraphExecEventRecordNodeSetEvent(stars->step_graph, stars->node_a, stars->cap_a);
+    cudaGraphExecEventRecordNodeSetEvent(stars->step_graph, stars->node_b, stars->cap_b);
+  }
+  stars->drop_profile_events();
+  *p2p_ms_total = total;
+  *p2p_launches = used;
+  return cuda_check("nbfmm_stars_profile_end");
+}
+
+int nbfmm_stars_kernel_launches(nbfmm_stars* stars, int num_steps, long long* launches) {
+  if (!stars || !launches) return fail(NBFMM_ERR_INVALID, "null argument");
+  if (num_steps <= 0) {
+    *launches = 0;
+    return NBFMM_OK;
+  }
+  if (!stars->step_graph) NBFMM_TRY(stars->build_graph());
+  const int outside = 2 /* import, step count */ + 2 /* export fate, fate keys */ +
+                      3 * stars->sort_passes(nbfmm_stars::fate_bits(num_steps)) + 1 /* head */ + 1 /* gather */;
+  *launches = (long long)num_steps * stars->kernels_per_step + outside;
+  return NBFMM_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,144 @@
+// engine.cuh -- shared definitions of the GB300 nbfmm engine (sm_103a).
+//
+// Data layout in HBM (one solver):
+//   particles, sorted by leaf cell (row-major key iy*B + ix):
+//     sorted4  float4 [max_n]   x, y, mass, original index (int bits)       16 B / particle
+//     seff     float2 [max_n]   near-field (and, after L2P, total) effect    8 B / particle
+//     skey     uint32 [max_n]   leaf cell key of each sorted particle        4 B / particle
+//   sort workspace: keys/values ping-pong (4 x 4 B / particle), per-tile digit counts, digit totals
+//   cells, compact per level (level l has D_l = B >> l cells per side, row-major, offset sum_{k<l} D_k^2):
+//     cell4    float4 [cells]   centre of mass x, y, mass, 0
+//     ceff     float2 [cells]   local (far-field) effect
+//   head     int32 [B*B + 1]  first sorted index of each leaf cell
+//   work     int2  [...]      non-empty (cell, target chunk) items for P2P
+// B = 2^(num_level + 1) leaf cells per side (source/nbfmm/core/solver.cu:19).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace nbfmm_gb300 {
+
+constexpr int kMaxLevels = 11;           // num_level in [0, 10], B <= 2048
+constexpr int kSortThreads = 256;        // radix sort CTA
+constexpr int kSortItems = 16;           // items per thread
+constexpr int kSortTile = kSortThreads * kSortItems;  // 4096 items per tile
+constexpr int kRadixMaxBits = 8;
+constexpr int kP2PThreads = 128;
+constexpr int kP2PTargetsPerThread = 2;
+constexpr int kP2PChunk = kP2PThreads * kP2PTargetsPerThread;  // targets per work item
+constexpr int kP2PTile = 512;            // source particles per shared-memory tile
+
+struct Geometry {
+  float xmin, ymin, xmax, ymax;  // position limits [x_min, y_min, x_max, y_max]
+  float cell_x, cell_y;          // leaf cell size, (max - min) / B in FP32 (predo.cu:112-113)
+  int num_level;                 // L
+  int base_dim;                  // B
+};
+
+struct Levels {
+  int count;                     // number of stored cell levels (max(L, 1))
+  int dim[kMaxLevels];           // cells per side of each level
+  int offset[kMaxLevels];        // first cell of each level in cell4 / ceff
+  int total;                     // total cells over all levels
+};
+
+// Leaf cell coordinate of one position component, floorf((v - lo) / cell) as in predo.cu:37-38, with IEEE
+// division; NaN and values below the domain give 0, values at or above the upper edge give B - 1.
+__device__ __forceinline__ int cell_coord(float v, float lo, float cell, int dim) {
+  const float f = floorf(__fdiv_rn(__fsub_rn(v, lo), cell));
+  if (!(f >= 0.0f)) return 0;
+  if (f >= (float)dim) return dim - 1;
+  return (int)f;
+}
+
+__device__ __forceinline__ uint32_t leaf_key(const Geometry& g, float x, float y) {
+  const int ix = cell_coord(x, g.xmin, g.cell_x, g.base_dim);
+  const int iy = cell_coord(y, g.ymin, g.cell_y, g.base_dim);
+  return (uint32_t)(ix + iy * g.base_dim);
+}
+
+// Outside the limits, the prune test of source/nbfmm/display/stars/prune.cu:40-41 (NaN is kept).
+__device__ __forceinline__ bool outside(const Geometry& g, float x, float y) {
+  return x < g.xmin || y < g.ymin || x > g.xmax || y > g.ymax;
+}
+
+// kernelFunction (include/nbfmm/core/kernel_function.hpp:29-40) with correctly rounded sqrt and division
+// and no fused multiply-add, so that it rounds like the reference compiled for a CPU. Used for the cell
+// stages, whose evaluation count is small.
+__device__ __forceinline__ float2 kernel_exact(float2 t, float2 s, float m, float eps) {
+  const float dx = __fsub_rn(s.x, t.x);
+  const float dy = __fsub_rn(s.y, t.y);
+  const float r = __fsqrt_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)));
+  const float tmp = __fdiv_rn(m, __fadd_rn(__fmul_rn(__fmul_rn(r, r), r), eps));
+  return make_float2(__fmul_rn(dx, tmp), __fmul_rn(dy, tmp));
+}
+
+// ---- launchers (defined in sort.cu / tree.cu / p2p.cu), all asynchronous on `stream` --------------------
+
+// Keys of positions given as float2 [n] (caller order); values = 0..n-1.
+void launch_keys_from_positions(const Geometry& g, const float2* pos, const int* d_n, uint32_t* keys,
+                                uint32_t* vals, int max_n, cudaStream_t stream);
+
+// Stable LSD radix sort of (keys, vals) on the low `key_bits` bits; n read from device memory.
+// Sorted output ends in (keys_a, vals_a). Returns 0, or -1 on an invalid configuration.
+int launch_radix_sort(uint32_t* keys_a, uint32_t* vals_a, uint32_t* keys_b, uint32_t* vals_b,
+                      uint32_t* counts, uint32_t* digit_total, const int* d_n, int max_n, int key_bits,
+                      cudaStream_t stream);
+
+// head[c] = first index with key >= c, c in [0, num_cells]; *d_n_alive = head[num_cells].
+void launch_head(const uint32_t* keys, const int* d_n, int num_cells, int* head, int* d_n_alive,
+                 cudaStream_t stream);
+
+// Work list of (cell, chunk) items over non-empty leaf cells; *d_work_count receives the count.
+void launch_worklist(const int* head, int num_cells, int2* work, int* d_work_count, cudaStream_t stream);
+
+// Gather the sorted particles from caller-order float2 positions and weights, and the leaf centres of
+// mass (P2M) of every leaf cell into level 0.
+void launch_gather_p2m(const Geometry& g, const int* head, const uint32_t* perm, const float2* pos,
+                       const float* w, float4* sorted4, float4* cell0, cudaStream_t stream);
+
+// P2M alone on already sorted particles (stage entry point).
+void launch_p2m(const Geometry& g, const int* head, const float4* sorted4, float4* cell0, cudaStream_t stream);
+
+// M2M, every level 1..L-1.
+void launch_m2m(const Levels& lv, float4* cell4, cudaStream_t stream);
+
+// M2L on every level; with `with_l2l` the parent effect is added on the way down (M2L + L2L fused).
+void launch_m2l(const Levels& lv, const float4* cell4, float2* ceff, float eps, bool with_l2l, cudaStream_t stream);
+
+// L2L alone (stage entry point).
+void launch_l2l(const Levels& lv, float2* ceff, cudaStream_t stream);
+
+// L2P alone: seff[i] += ceff[level 0][skey[i]] (stage entry point).
+void launch_l2p(const int* d_n, const uint32_t* skey, const float2* ceff0, float2* seff, int max_n, cudaStream_t stream);
+
+// postdo alone: eff_origin[perm[i]] = seff[i] (stage entry point).
+void launch_postdo(const int* d_n, const uint32_t* perm, const float2* seff, float2* eff_origin, int max_n,
+                   cudaStream_t stream);
+
+// Sorted leaf keys from head (stage entry point helper): skey[i] = cell of i.
+void launch_keys_from_head(const int* head, int num_cells, uint32_t* skey, cudaStream_t stream);
+
+enum P2PEpilogue { kStoreSorted = 0, kSolve = 1, kVerlet = 2 };
+
+struct P2PArgs {
+  const float4* sorted4;   // sorted particles
+  const int* head;         // leaf heads
+  const int2* work;        // (cell, chunk) items
+  const int* d_work_count;
+  int* d_work_next;        // dynamic scheduling counter, zero before launch
+  int base_dim;
+  float eps;
+  const float2* ceff0;     // level-0 local effects (kSolve, kVerlet), may be null when num_level == 0
+  float2* seff;            // kStoreSorted: sorted effects
+  float2* eff_origin;      // kSolve: effects in caller order
+  const float2* sprev;     // kVerlet: sorted previous positions
+  float4* state4;          // kVerlet: new state (x', y', m, original index)
+  float2* state_prev;      // kVerlet: new previous positions
+  float tick;              // kVerlet: tick * sqrt(G)
+};
+
+void launch_p2p(const P2PArgs& a, P2PEpilogue mode, int num_sms, cudaStream_t stream);
+
+}  // namespace nbfmm_gb300

@@ -1,0 +1,276 @@
+// sort.cu -- preassign for the GB300 engine: leaf keys, a stable LSD radix sort by leaf cell, cell heads
+// and the P2P work list.
+//
+// Replaces predo (source/nbfmm/core/solver/predo.cu:105-135): computeParticleIndex (predo.cu:26-39),
+// the iota + thrust::sort_by_key on int2 keys under the row-major operator< (predo.cu:123-127,
+// include/nbfmm/utility/operator.hpp:107-109) and extractHead (predo.cu:49-74). The row-major int2 order
+// equals the order of the integer key iy*B + ix, and cub's merge sort keeps equal keys in input order, so a
+// stable radix sort on that key reproduces the reference's permutation bit for bit.
+//
+// Sort design: per pass, an upsweep writes each 4096-item tile's digit histogram, one CTA per digit scans
+// its row of tile counts, and a downsweep ranks each tile's items stably (warp match + per-warp digit
+// counters in shared memory) and scatters them. Every kernel reads the element count from device memory,
+// so the same launches serve any n <= max_n without a host round trip (and can be captured in a graph).
+#include "engine.cuh"
+
+namespace nbfmm_gb300 {
+
+namespace {
+
+__device__ __forceinline__ int num_tiles(int n) { return (n + kSortTile - 1) / kSortTile; }
+
+// Exclusive scan over a 256-thread block; returns the block total in *total.
+__device__ __forceinline__ uint32_t block_exclusive_scan_256(uint32_t v, uint32_t* warp_sums, uint32_t* total) {
+  const int lane = threadIdx.x & 31;
+  const int warp = threadIdx.x >> 5;
+  uint32_t x = v;
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    const uint32_t y = __shfl_up_sync(0xffffffffu, x, d);
+    if (lane >= d) x += y;
+  }
+  if (lane == 31) warp_sums[warp] = x;
+  __syncthreads();
+  if (warp == 0) {
+    uint32_t s = (lane < kSortThreads / 32) ? warp_sums[lane] : 0u;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xffffffffu, s, d);
+      if (lane >= d) s += y;
+    }
+    if (lane < kSortThreads / 32) warp_sums[lane] = s;  // inclusive warp prefix
+  }
+  __syncthreads();
+  const uint32_t warp_prefix = (warp > 0) ? warp_sums[warp - 1] : 0u;
+  *total = warp_sums[kSortThreads / 32 - 1];
+  __syncthreads();
+  return warp_prefix + x - v;
+}
+
+__global__ void keys_from_positions_kernel(Geometry g, const float2* __restrict__ pos, const int* __restrict__ d_n,
+                                           uint32_t* __restrict__ keys, uint32_t* __restrict__ vals) {
+  const int n = *d_n;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const float2 p = pos[i];
+    keys[i] = leaf_key(g, p.x, p.y);
+    vals[i] = (uint32_t)i;
+  }
+}
+
+__global__ void __launch_bounds__(kSortThreads)
+radix_upsweep_kernel(const uint32_t* __restrict__ keys, const int* __restrict__ d_n, int shift, int bits,
+                     uint32_t* __restrict__ counts, int max_tiles) {
+  __shared__ uint32_t hist[1 << kRadixMaxBits];
+  const int n = *d_n;
+  const int t = blockIdx.x;
+  if (t >= num_tiles(n)) return;
+  const int nd = 1 << bits;
+  const uint32_t mask = (uint32_t)nd - 1u;
+  for (int d = threadIdx.x; d < nd; d += kSortThreads) hist[d] = 0u;
+  __syncthreads();
+  const int base = t * kSortTile;
+  const int end = min(base + kSortTile, n);
+  for (int i = base + threadIdx.x; i < end; i += kSortThreads) {
+    atomicAdd(&hist[(keys[i] >> shift) & mask], 1u);
+  }
+  __syncthreads();
+  for (int d = threadIdx.x; d < nd; d += kSortThreads) counts[(size_t)d * max_tiles + t] = hist[d];
+}
+
+// One CTA per digit: exclusive scan of that digit's tile counts; the digit's total goes to digit_total.
+__global__ void __launch_bounds__(kSortThreads)
+radix_scan_kernel(uint32_t* __restrict__ counts, uint32_t* __restrict__ digit_total, const int* __restrict__ d_n,
+                  int max_tiles) {
+  __shared__ uint32_t warp_sums[kSortThreads / 32];
+  const int nt = num_tiles(*d_n);
+  uint32_t* row = counts + (size_t)blockIdx.x * max_tiles;
+  uint32_t carry = 0;
+  for (int base = 0; base < nt; base += kSortThreads * 4) {
+    const int i0 = base + threadIdx.x * 4;
+    uint32_t v[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) v[k] = (i0 + k < nt) ? row[i0 + k] : 0u;
+    const uint32_t local = v[0] + v[1] + v[2] + v[3];
+    uint32_t total;
+    uint32_t run = carry + block_exclusive_scan_256(local, warp_sums, &total);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      if (i0 + k < nt) row[i0 + k] = run;
+      run += v[k];
+    }
+    carry += total;
+  }
+  if (threadIdx.x == 0) digit_total[blockIdx.x] = carry;
+}
+
+__global__ void __launch_bounds__(kSortThreads)
+radix_downsweep_kernel(const uint32_t* __restrict__ keys_in, const uint32_t* __restrict__ vals_in,
+                       uint32_t* __restrict__ keys_out, uint32_t* __restrict__ vals_out,
+                       const int* __restrict__ d_n, int shift, int bits, const uint32_t* __restrict__ counts,
+                       const uint32_t* __restrict__ digit_total, int max_tiles) {
+  constexpr int kWarps = kSortThreads / 32;
+  __shared__ uint32_t warp_hist[kWarps][1 << kRadixMaxBits];
+  __shared__ uint32_t digit_base[1 << kRadixMaxBits];
+  __shared__ uint32_t warp_sums[kWarps];
+  const int n = *d_n;
+  const int t = blockIdx.x;
+  if (t >= num_tiles(n)) return;
+  const int nd = 1 << bits;
+  const uint32_t mask = (uint32_t)nd - 1u;
+  const int lane = threadIdx.x & 31;
+  const int warp = threadIdx.x >> 5;
+
+  // Start of every digit in the output: exclusive scan of the digit totals.
+  {
+    const uint32_t v = (threadIdx.x < nd) ? digit_total[threadIdx.x] : 0u;
+    uint32_t total;
+    const uint32_t ex = block_exclusive_scan_256(v, warp_sums, &total);
+    if (threadIdx.x < nd) digit_base[threadIdx.x] = ex;
+  }
+  for (int d = lane; d < nd; d += 32) warp_hist[warp][d] = 0u;
+  __syncwarp();
+
+  // Warp `warp` owns items [warp*512, warp*512 + 512) of the tile, in 16 rounds of 32 consecutive items.
+  const int base = t * kSortTile + warp * (32 * kSortItems);
+  const unsigned lt_mask = (1u << lane) - 1u;
+  uint32_t key[kSortItems], val[kSortItems], rank[kSortItems];
+#pragma unroll
+  for (int r = 0; r < kSortItems; ++r) {
+    const int i = base + r * 32 + lane;
+    const bool valid = i < n;
+    key[r] = valid ? keys_in[i] : 0u;
+    val[r] = valid ? vals_in[i] : 0u;
+    const uint32_t digit = valid ? ((key[r] >> shift) & mask) : (uint32_t)nd;  // nd marks an empty slot
+    const unsigned peers = __match_any_sync(0xffffffffu, digit);
+    const uint32_t before = valid ? warp_hist[warp][digit] : 0u;
+    __syncwarp();
+    if (valid && lane == __ffs(peers) - 1) warp_hist[warp][digit] = before + __popc(peers);
+    __syncwarp();
+    rank[r] = before + __popc(peers & lt_mask);
+  }
+  __syncthreads();
+  // Per digit, exclusive prefix over the warps (warp order is item order within the tile).
+  for (int d = threadIdx.x; d < nd; d += kSortThreads) {
+    uint32_t run = digit_base[d] + counts[(size_t)d * max_tiles + t];
+#pragma unroll
+    for (int w = 0; w < kWarps; ++w) {
+      const uint32_t c = warp_hist[w][d];
+      warp_hist[w][d] = run;
+      run += c;
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int r = 0; r < kSortItems; ++r) {
+    const int i = base + r * 32 + lane;
+    if (i < n) {
+      const uint32_t digit = (key[r] >> shift) & mask;
+      const uint32_t dst = warp_hist[warp][digit] + rank[r];
+      keys_out[dst] = key[r];
+      vals_out[dst] = val[r];
+    }
+  }
+}
+
+__global__ void head_kernel(const uint32_t* __restrict__ keys, const int* __restrict__ d_n, int num_cells,
+                            int* __restrict__ head, int* __restrict__ d_n_alive) {
+  const int n = *d_n;
+  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c <= num_cells; c += gridDim.x * blockDim.x) {
+    int lo = 0, hi = n;
+    while (lo < hi) {
+      const int mid = (lo + hi) >> 1;
+      if (keys[mid] < (uint32_t)c) lo = mid + 1; else hi = mid;
+    }
+    head[c] = lo;
+    if (c == num_cells && d_n_alive) *d_n_alive = lo;
+  }
+}
+
+__global__ void worklist_kernel(const int* __restrict__ head, int num_cells, int2* __restrict__ work,
+                                int* __restrict__ d_work_count) {
+  const int lane = threadIdx.x & 31;
+  // Whole warps iterate together so that the warp-wide scan below sees every lane.
+  for (int base = blockIdx.x * blockDim.x; base < num_cells; base += gridDim.x * blockDim.x) {
+    const int c = base + threadIdx.x;
+    int chunks = 0;
+    if (c < num_cells) {
+      const int nt = head[c + 1] - head[c];
+      chunks = (nt + kP2PChunk - 1) / kP2PChunk;
+    }
+    int incl = chunks;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, incl, d);
+      if (lane >= d) incl += y;
+    }
+    int start = 0;
+    if (lane == 31 && incl > 0) start = atomicAdd(d_work_count, incl);
+    start = __shfl_sync(0xffffffffu, start, 31);
+    for (int k = 0; k < chunks; ++k) work[start + incl - chunks + k] = make_int2(c, k);
+  }
+}
+
+__global__ void keys_from_head_kernel(const int* __restrict__ head, int num_cells, uint32_t* __restrict__ skey) {
+  const int n = head[num_cells];
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    int lo = 0, hi = num_cells;  // first c with head[c] > i, minus one
+    while (lo < hi) {
+      const int mid = (lo + hi) >> 1;
+      if (head[mid] <= i) lo = mid + 1; else hi = mid;
+    }
+    skey[i] = (uint32_t)(lo - 1);
+  }
+}
+
+int grid_for(int n, int threads, int cap) {
+  long long g = ((long long)n + threads - 1) / threads;
+  if (g < 1) g = 1;
+  if (g > cap) g = cap;
+  return (int)g;
+}
+
+}  // namespace
+
+void launch_keys_from_positions(const Geometry& g, const float2* pos, const int* d_n, uint32_t* keys,
+                                uint32_t* vals, int max_n, cudaStream_t stream) {
+  keys_from_positions_kernel<<<grid_for(max_n, 256, 152 * 16), 256, 0, stream>>>(g, pos, d_n, keys, vals);
+}
+
+int launch_radix_sort(uint32_t* keys_a, uint32_t* vals_a, uint32_t* keys_b, uint32_t* vals_b,
+                      uint32_t* counts, uint32_t* digit_total, const int* d_n, int max_n, int key_bits,
+                      cudaStream_t stream) {
+  if (key_bits <= 0) return 0;
+  const int max_tiles = (max_n + kSortTile - 1) / kSortTile;
+  const int passes = (key_bits + kRadixMaxBits - 1) / kRadixMaxBits;
+  const int per_pass = (key_bits + passes - 1) / passes;
+  uint32_t* kin = keys_a; uint32_t* vin = vals_a;
+  uint32_t* kout = keys_b; uint32_t* vout = vals_b;
+  int shift = 0;
+  for (int p = 0; p < passes; ++p) {
+    const int bits = (shift + per_pass <= key_bits) ? per_pass : key_bits - shift;
+    radix_upsweep_kernel<<<max_tiles, kSortThreads, 0, stream>>>(kin, d_n, shift, bits, counts, max_tiles);
+    radix_scan_kernel<<<1 << bits, kSortThreads, 0, stream>>>(counts, digit_total, d_n, max_tiles);
+    radix_downsweep_kernel<<<max_tiles, kSortThreads, 0, stream>>>(kin, vin, kout, vout, d_n, shift, bits, counts,
+                                                                   digit_total, max_tiles);
+    shift += bits;
+    uint32_t* tk = kin; kin = kout; kout = tk;
+    uint32_t* tv = vin; vin = vout; vout = tv;
+  }
+  return (kin == keys_a) ? 0 : 1;  // which buffer pair holds the result
+}
+
+void launch_head(const uint32_t* keys, const int* d_n, int num_cells, int* head, int* d_n_alive,
+                 cudaStream_t stream) {
+  head_kernel<<<grid_for(num_cells + 1, 256, 152 * 16), 256, 0, stream>>>(keys, d_n, num_cells, head, d_n_alive);
+}
+
+void launch_worklist(const int* head, int num_cells, int2* work, int* d_work_count, cudaStream_t stream) {
+  cudaMemsetAsync(d_work_count, 0, sizeof(int), stream);
+  worklist_kernel<<<grid_for(num_cells, 256, 152 * 8), 256, 0, stream>>>(head, num_cells, work, d_work_count);
+}
+
+void launch_keys_from_head(const int* head, int num_cells, uint32_t* skey, cudaStream_t stream) {
+  keys_from_head_kernel<<<152 * 8, 256, 0, stream>>>(head, num_cells, skey);
+}
+
+}  // namespace nbfmm_gb300

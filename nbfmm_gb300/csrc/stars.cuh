@@ -1,0 +1,37 @@
+// stars.cuh -- device counters and launchers of the time-stepping path (stars.cu).
+#pragma once
+
+#include "engine.cuh"
+
+namespace nbfmm_gb300 {
+
+// Counters kept in device memory so that a step needs no host round trip and can be replayed from a graph.
+struct StepCounters {
+  int* num_star;   // public number of stars (num_star_ of the reference's Stars)
+  int* n_import;   // stars at the start of the current update call
+  int* n_cur;      // stars in the internal state
+  int* n_alive;    // live stars after this step's key pass (head[B*B])
+  int* step;       // 1-based step index within the call
+  int* prune;      // 0 on the first step of a call (its input was pruned by the previous call)
+  int* num_steps;  // steps of the current call
+};
+
+void launch_set_int(int* p, int v, cudaStream_t stream);
+void launch_import(const StepCounters& sc, const float2* cur, const float2* prev, const float* w, float4* state4,
+                   float2* state_prev, float* w_by_orig, int max_n, cudaStream_t stream);
+void launch_keys_from_state(const Geometry& g, const StepCounters& sc, const float4* state4, const float2* state_prev,
+                            uint32_t dead_key, uint32_t* keys, uint32_t* vals, float2* grave_cur, float2* grave_prev,
+                            int* fate, int max_n, cudaStream_t stream);
+void launch_gather_state_p2m(const Geometry& g, const int* head, const uint32_t* perm, const float4* state4,
+                             const float2* state_prev, float4* sorted4, float2* sprev, float4* cell0,
+                             cudaStream_t stream);
+void launch_finish_step(const StepCounters& sc, cudaStream_t stream);
+void launch_export_fate(const Geometry& g, const StepCounters& sc, const float4* state4, const float2* state_prev,
+                        float2* grave_cur, float2* grave_prev, int* fate, int max_n, cudaStream_t stream);
+void launch_fate_keys(const StepCounters& sc, const int* fate, uint32_t* keys, uint32_t* vals, int max_n,
+                      cudaStream_t stream);
+void launch_export_gather(const StepCounters& sc, const uint32_t* order, const float2* grave_cur,
+                          const float2* grave_prev, const float* w_by_orig, float2* cur, float2* prev, float* w,
+                          int max_n, cudaStream_t stream);
+
+}  // namespace nbfmm_gb300

@@ -1,0 +1,234 @@
+// tree.cu -- cell stages of the GB300 engine: gather + P2M, M2M, M2L (+ L2L), and the stage-alone L2L, L2P
+// and postdo used by the stage entry points.
+//
+// Reference stages replaced (source/nbfmm/core/solver/):
+//   permuteInputVector  predo.cu:86-100    fused with P2M below (one pass over the sorted particles)
+//   p2m                 p2m.cu:24-110      segmented sums per leaf cell by one warp, no reduce_by_key, no host sync
+//   m2m                 m2m.cu:22-74       one thread per parent cell, compact per-level layout
+//   m2l                 m2l.cu:24-81       16x16 target tile per CTA with its 20x20 source halo in shared memory
+//   l2l                 l2l.cu:21-56       fused into M2L on the way down (child = m2l + parent)
+//   l2p                 l2p.cu:23-48       stage-alone here; fused into the P2P epilogue on the solve path
+//   permuteOutputVector postdo.cu:22-45    stage-alone here; fused into the P2P epilogue on the solve path
+// The cell arithmetic uses correctly rounded operations without fused multiply-add, in the reference's
+// order, so cell values round like the reference compiled for a CPU.
+#include "engine.cuh"
+
+namespace nbfmm_gb300 {
+
+namespace {
+
+__device__ __forceinline__ float warp_sum(float v) {
+#pragma unroll
+  for (int d = 16; d >= 1; d >>= 1) v = __fadd_rn(v, __shfl_xor_sync(0xffffffffu, v, d));
+  return v;
+}
+
+__device__ __forceinline__ float4 centre_of_mass(float sx, float sy, float sw, bool nonempty) {
+  if (!nonempty) return make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+  return make_float4(__fdiv_rn(sx, sw), __fdiv_rn(sy, sw), sw, 0.0f);
+}
+
+__global__ void gather_p2m_kernel(int num_cells, const int* __restrict__ head, const uint32_t* __restrict__ perm,
+                                  const float2* __restrict__ pos, const float* __restrict__ w,
+                                  float4* __restrict__ sorted4, float4* __restrict__ cell0) {
+  const int lane = threadIdx.x & 31;
+  const int nwarps = (gridDim.x * blockDim.x) >> 5;
+  for (int c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; c < num_cells; c += nwarps) {
+    const int h0 = head[c], h1 = head[c + 1];
+    float sx = 0.0f, sy = 0.0f, sw = 0.0f;
+    for (int i = h0 + lane; i < h1; i += 32) {
+      const uint32_t p = perm[i];
+      const float2 q = pos[p];
+      const float m = w[p];
+      sorted4[i] = make_float4(q.x, q.y, m, __int_as_float((int)p));
+      sx = __fadd_rn(sx, __fmul_rn(q.x, m));
+      sy = __fadd_rn(sy, __fmul_rn(q.y, m));
+      sw = __fadd_rn(sw, m);
+    }
+    sx = warp_sum(sx);
+    sy = warp_sum(sy);
+    sw = warp_sum(sw);
+    if (lane == 0) cell0[c] = centre_of_mass(sx, sy, sw, h1 > h0);
+  }
+}
+
+__global__ void p2m_kernel(int num_cells, const int* __restrict__ head, const float4* __restrict__ sorted4,
+                           float4* __restrict__ cell0) {
+  const int lane = threadIdx.x & 31;
+  const int nwarps = (gridDim.x * blockDim.x) >> 5;
+  for (int c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; c < num_cells; c += nwarps) {
+    const int h0 = head[c], h1 = head[c + 1];
+    float sx = 0.0f, sy = 0.0f, sw = 0.0f;
+    for (int i = h0 + lane; i < h1; i += 32) {
+      const float4 q = sorted4[i];
+      sx = __fadd_rn(sx, __fmul_rn(q.x, q.z));
+      sy = __fadd_rn(sy, __fmul_rn(q.y, q.z));
+      sw = __fadd_rn(sw, q.z);
+    }
+    sx = warp_sum(sx);
+    sy = warp_sum(sy);
+    sw = warp_sum(sw);
+    if (lane == 0) cell0[c] = centre_of_mass(sx, sy, sw, h1 > h0);
+  }
+}
+
+// m2m.cu:40-53: children (x,y), (x+1,y), (x,y+1), (x+1,y+1) summed left to right; zero mass -> (0,0).
+__global__ void m2m_kernel(float4* __restrict__ cell4, int off_c, int dim_c, int off_p, int dim_p) {
+  const int total = dim_p * dim_p;
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < total; k += gridDim.x * blockDim.x) {
+    const int px = k % dim_p, py = k / dim_p;
+    const int c0 = off_c + (2 * py) * dim_c + 2 * px;
+    const float4 a = cell4[c0], b = cell4[c0 + 1], c = cell4[c0 + dim_c], d = cell4[c0 + dim_c + 1];
+    float sx = __fmul_rn(a.x, a.z);
+    float sy = __fmul_rn(a.y, a.z);
+    sx = __fadd_rn(sx, __fmul_rn(b.x, b.z));
+    sy = __fadd_rn(sy, __fmul_rn(b.y, b.z));
+    sx = __fadd_rn(sx, __fmul_rn(c.x, c.z));
+    sy = __fadd_rn(sy, __fmul_rn(c.y, c.z));
+    sx = __fadd_rn(sx, __fmul_rn(d.x, d.z));
+    sy = __fadd_rn(sy, __fmul_rn(d.y, d.z));
+    const float sw = __fadd_rn(__fadd_rn(__fadd_rn(a.z, b.z), c.z), d.z);
+    float4 out = make_float4(0.0f, 0.0f, sw, 0.0f);
+    if (sw != 0.0f) {
+      out.x = __fdiv_rn(sx, sw);
+      out.y = __fdiv_rn(sy, sw);
+    }
+    cell4[off_p + k] = out;
+  }
+}
+
+constexpr int kM2LTile = 16;
+constexpr int kM2LHalo = kM2LTile + 4;
+
+// m2l.cu:24-60 for one level. Each CTA owns a 16x16 tile of target cells (tile origin even, so the
+// children of the parents' neighbours lie in the 20x20 halo around it). With add_parent the parent's
+// effect is added afterwards (l2l.cu:33-35): child = m2l + parent.
+__global__ void __launch_bounds__(kM2LTile * kM2LTile)
+m2l_kernel(const float4* __restrict__ cell4, float2* __restrict__ ceff, int off, int dim, int off_parent,
+           int dim_parent, int add_parent, float eps) {
+  __shared__ float4 halo[kM2LHalo][kM2LHalo];
+  const int x0 = blockIdx.x * kM2LTile, y0 = blockIdx.y * kM2LTile;
+  const int tid = threadIdx.y * kM2LTile + threadIdx.x;
+  for (int k = tid; k < kM2LHalo * kM2LHalo; k += kM2LTile * kM2LTile) {
+    const int hx = k % kM2LHalo, hy = k / kM2LHalo;
+    const int gx = x0 - 2 + hx, gy = y0 - 2 + hy;
+    halo[hy][hx] = (gx >= 0 && gx < dim && gy >= 0 && gy < dim) ? cell4[off + gy * dim + gx]
+                                                                 : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+  }
+  __syncthreads();
+  const int tx = x0 + threadIdx.x, ty = y0 + threadIdx.y;
+  if (tx >= dim || ty >= dim) return;
+  const float4 t = halo[ty - y0 + 2][tx - x0 + 2];
+  const float2 tp = make_float2(t.x, t.y);
+  const int px = tx & ~1, py = ty & ~1;
+  float ex = 0.0f, ey = 0.0f;
+  for (int y = py - 2; y < py + 4; ++y) {
+    if (y < 0 || y >= dim) continue;
+    for (int x = px - 2; x < px + 4; ++x) {
+      if (x < 0 || x >= dim) continue;
+      if (abs(x - tx) > 1 || abs(y - ty) > 1) {
+        const float4 s = halo[y - y0 + 2][x - x0 + 2];
+        const float2 k = kernel_exact(tp, make_float2(s.x, s.y), s.z, eps);
+        ex = __fadd_rn(ex, k.x);
+        ey = __fadd_rn(ey, k.y);
+      }
+    }
+  }
+  if (add_parent) {
+    const float2 p = ceff[off_parent + (ty >> 1) * dim_parent + (tx >> 1)];
+    ex = __fadd_rn(ex, p.x);
+    ey = __fadd_rn(ey, p.y);
+  }
+  ceff[off + ty * dim + tx] = make_float2(ex, ey);
+}
+
+__global__ void l2l_kernel(float2* __restrict__ ceff, int off, int dim, int off_parent, int dim_parent) {
+  const int total = dim * dim;
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < total; k += gridDim.x * blockDim.x) {
+    const int x = k % dim, y = k / dim;
+    const float2 p = ceff[off_parent + (y >> 1) * dim_parent + (x >> 1)];
+    float2 e = ceff[off + k];
+    e.x = __fadd_rn(e.x, p.x);
+    e.y = __fadd_rn(e.y, p.y);
+    ceff[off + k] = e;
+  }
+}
+
+__global__ void l2p_kernel(const int* __restrict__ d_n, const uint32_t* __restrict__ skey,
+                           const float2* __restrict__ ceff0, float2* __restrict__ seff) {
+  const int n = *d_n;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const float2 c = ceff0[skey[i]];
+    float2 e = seff[i];
+    e.x = __fadd_rn(e.x, c.x);
+    e.y = __fadd_rn(e.y, c.y);
+    seff[i] = e;
+  }
+}
+
+__global__ void postdo_kernel(const int* __restrict__ d_n, const uint32_t* __restrict__ perm,
+                              const float2* __restrict__ seff, float2* __restrict__ eff_origin) {
+  const int n = *d_n;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    eff_origin[perm[i]] = seff[i];
+  }
+}
+
+int grid_for(long long n, int threads, int cap) {
+  long long g = (n + threads - 1) / threads;
+  if (g < 1) g = 1;
+  if (g > cap) g = cap;
+  return (int)g;
+}
+
+}  // namespace
+
+void launch_gather_p2m(const Geometry& g, const int* head, const uint32_t* perm, const float2* pos,
+                       const float* w, float4* sorted4, float4* cell0, cudaStream_t stream) {
+  const int cells = g.base_dim * g.base_dim;
+  gather_p2m_kernel<<<grid_for((long long)cells * 32, 256, 152 * 16), 256, 0, stream>>>(cells, head, perm, pos, w,
+                                                                                        sorted4, cell0);
+}
+
+void launch_p2m(const Geometry& g, const int* head, const float4* sorted4, float4* cell0, cudaStream_t stream) {
+  const int cells = g.base_dim * g.base_dim;
+  p2m_kernel<<<grid_for((long long)cells * 32, 256, 152 * 16), 256, 0, stream>>>(cells, head, sorted4, cell0);
+}
+
+void launch_m2m(const Levels& lv, float4* cell4, cudaStream_t stream) {
+  for (int l = 1; l < lv.count; ++l) {
+    const int total = lv.dim[l] * lv.dim[l];
+    m2m_kernel<<<grid_for(total, 256, 152 * 8), 256, 0, stream>>>(cell4, lv.offset[l - 1], lv.dim[l - 1],
+                                                                  lv.offset[l], lv.dim[l]);
+  }
+}
+
+void launch_m2l(const Levels& lv, const float4* cell4, float2* ceff, float eps, bool with_l2l, cudaStream_t stream) {
+  for (int l = lv.count - 1; l >= 0; --l) {
+    const int dim = lv.dim[l];
+    const dim3 grid((dim + kM2LTile - 1) / kM2LTile, (dim + kM2LTile - 1) / kM2LTile);
+    const int has_parent = (with_l2l && l + 1 < lv.count) ? 1 : 0;
+    const int lp = has_parent ? l + 1 : l;
+    m2l_kernel<<<grid, dim3(kM2LTile, kM2LTile), 0, stream>>>(cell4, ceff, lv.offset[l], dim, lv.offset[lp],
+                                                               lv.dim[lp], has_parent, eps);
+  }
+}
+
+void launch_l2l(const Levels& lv, float2* ceff, cudaStream_t stream) {
+  for (int l = lv.count - 2; l >= 0; --l) {
+    const int total = lv.dim[l] * lv.dim[l];
+    l2l_kernel<<<grid_for(total, 256, 152 * 8), 256, 0, stream>>>(ceff, lv.offset[l], lv.dim[l], lv.offset[l + 1],
+                                                                  lv.dim[l + 1]);
+  }
+}
+
+void launch_l2p(const int* d_n, const uint32_t* skey, const float2* ceff0, float2* seff, int max_n, cudaStream_t stream) {
+  l2p_kernel<<<grid_for(max_n, 256, 152 * 16), 256, 0, stream>>>(d_n, skey, ceff0, seff);
+}
+
+void launch_postdo(const int* d_n, const uint32_t* perm, const float2* seff, float2* eff_origin, int max_n,
+                   cudaStream_t stream) {
+  postdo_kernel<<<grid_for(max_n, 256, 152 * 16), 256, 0, stream>>>(d_n, perm, seff, eff_origin);
+}
+
+}  // namespace nbfmm_gb300

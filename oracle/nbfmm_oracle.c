@@ -1,0 +1,485 @@
+/*
+ * nbfmm_oracle.c -- CPU restatement of the nbfmm 2D monopole FMM (TEST INFRASTRUCTURE ONLY).
+ *
+ * Only the tests, __graft_entry__.smoke() and the CPU-baseline leg of bench.py load this library, and only
+ * as the checker; the engine never calls it. See nbfmm_oracle.h for the stage list, the reference lines each
+ * function follows, and the three reference defects that are neutralised here.
+ *
+ * Built with -ffp-contract=off so that x86 and Arm hosts round identically; where the engine fuses a
+ * multiply-add on purpose the restatement calls fmaf() explicitly.
+ */
+#include "nbfmm_oracle.h"
+
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+int orc_num_threads(void) {
+#ifdef _OPENMP
+  return omp_get_max_threads();
+#else
+  return 1;
+#endif
+}
+
+/* include/nbfmm/core/kernel_function.hpp:29-40. The reference fixes eps = 1e-1; here it is a parameter. */
+void orc_kernel_function(float tx, float ty, float sx, float sy, float m, float eps, float* ax, float* ay) {
+  const float dx = sx - tx;
+  const float dy = sy - ty;
+  const float r = sqrtf(dx * dx + dy * dy);
+  const float tmp = m / (r * r * r + eps);
+  *ax = dx * tmp;
+  *ay = dy * tmp;
+}
+
+int orc_base_dim(int num_level) { return 1 << (num_level + 1); }
+
+/* predo.cu:37-38 with the cell size of predo.cu:112-113 (a float divided by the int base_dim). */
+static inline int cell_coord(float v, float lo, float cell, int dim) {
+  const float f = floorf((v - lo) / cell);
+  if (!(f >= 0.0f)) return 0;            /* NaN and values below the domain land in cell 0 */
+  if (f >= (float)dim) return dim - 1;   /* the upper edge and beyond land in the last cell */
+  return (int)f;
+}
+
+void orc_cell_index(const float limits[4], int base_dim, float x, float y, int* ix, int* iy) {
+  const float cx = (limits[2] - limits[0]) / (float)base_dim;
+  const float cy = (limits[3] - limits[1]) / (float)base_dim;
+  *ix = cell_coord(x, limits[0], cx, base_dim);
+  *iy = cell_coord(y, limits[1], cy, base_dim);
+}
+
+/*
+ * predo.cu:105-135. The reference sorts int2 keys with thrust::sort_by_key under the row-major operator<
+ * (operator.hpp:107-109: y first, then x); cub's merge sort keeps equal keys in input order, so the result
+ * equals a stable counting sort on key = iy*B + ix, which is what this does. head[c] is the first sorted
+ * index whose key is >= c (extractHead, predo.cu:49-74, with every entry written).
+ */
+void orc_predo(int n, int num_level, const float limits[4], const float* pos, const float* w,
+               int* index, int* perm, int* head, float* pos_sorted, float* w_sorted) {
+  const int B = orc_base_dim(num_level);
+  const int C = B * B;
+  int* key = (int*)malloc(sizeof(int) * (size_t)(n > 0 ? n : 1));
+  int* cnt = (int*)calloc((size_t)C + 1, sizeof(int));
+  for (int i = 0; i < n; ++i) {
+    int ix, iy;
+    orc_cell_index(limits, B, pos[2 * i], pos[2 * i + 1], &ix, &iy);
+    key[i] = ix + iy * B;
+    cnt[key[i]]++;
+  }
+  int run = 0;
+  for (int c = 0; c < C; ++c) {
+    head[c] = run;
+    run += cnt[c];
+  }
+  head[C] = run;
+  for (int c = 0; c < C; ++c) cnt[c] = head[c];
+  for (int i = 0; i < n; ++i) perm[cnt[key[i]]++] = i; /* stable: input order within a cell */
+  for (int i = 0; i < n; ++i) {
+    const int p = perm[i];
+    index[2 * i] = key[p] % B;
+    index[2 * i + 1] = key[p] / B;
+    pos_sorted[2 * i] = pos[2 * p];
+    pos_sorted[2 * i + 1] = pos[2 * p + 1];
+    w_sorted[i] = w[p];
+  }
+  free(key);
+  free(cnt);
+}
+
+/* p2p.cu:30-69 (p2pNaive): rows y-1..y+1, cells x-1..x+1, particles in sorted order, self skipped. */
+void orc_p2p_naive(int n, int base_dim, const float* pos, const float* w, const int* index, const int* head,
+                   float eps, float* eff) {
+  const int B = base_dim;
+#pragma omp parallel for schedule(dynamic, 256)
+  for (int i = 0; i < n; ++i) {
+    const int px = index[2 * i], py = index[2 * i + 1];
+    const float tx = pos[2 * i], ty = pos[2 * i + 1];
+    float ex = 0.0f, ey = 0.0f;
+    for (int y = py - 1; y <= py + 1; ++y) {
+      for (int x = px - 1; x <= px + 1; ++x) {
+        if (x < 0 || x >= B || y < 0 || y >= B) continue;
+        const int c = x + y * B;
+        for (int k = head[c]; k < head[c + 1]; ++k) {
+          if (k == i) continue;
+          float ax, ay;
+          orc_kernel_function(tx, ty, pos[2 * k], pos[2 * k + 1], w[k], eps, &ax, &ay);
+          ex += ax;
+          ey += ay;
+        }
+      }
+    }
+    eff[2 * i] = ex;
+    eff[2 * i + 1] = ey;
+  }
+}
+
+/* p2p.cu:82-161 (p2pBlock): per row a contiguous range, 64-wide chunks, tree reduction per chunk. */
+void orc_p2p_block(int n, int base_dim, const float* pos, const float* w, const int* index, const int* head,
+                   float eps, float* eff) {
+  const int B = base_dim;
+  enum { kChunk = 64 };
+#pragma omp parallel for schedule(dynamic, 64)
+  for (int i = 0; i < n; ++i) {
+    const int px = index[2 * i], py = index[2 * i + 1];
+    const float tx = pos[2 * i], ty = pos[2 * i + 1];
+    const int left = (px - 1 > 0) ? px - 1 : 0;
+    const int right = (px + 1 < B) ? px + 1 : B - 1;
+    float ex = 0.0f, ey = 0.0f;
+    float tmpx[kChunk], tmpy[kChunk];
+    for (int row = 0; row < 3; ++row) {
+      const int y = py + row - 1;
+      int start = 0, end = 0;
+      if (y >= 0 && y < B) {
+        start = head[left + y * B];
+        end = head[right + y * B + 1];
+      }
+      const int loops = (end - start) / kChunk + 1;
+      for (int l = 0; l < loops; ++l) {
+        for (int r = 0; r < kChunk; ++r) {
+          const int k = start + l * kChunk + r;
+          if (k < end && k != i) {
+            orc_kernel_function(tx, ty, pos[2 * k], pos[2 * k + 1], w[k], eps, &tmpx[r], &tmpy[r]);
+          } else {
+            tmpx[r] = 0.0f;
+            tmpy[r] = 0.0f;
+          }
+        }
+        for (int half = kChunk / 2; half >= 1; half /= 2) {
+          for (int r = 0; r < half; ++r) {
+            tmpx[r] += tmpx[r + half];
+            tmpy[r] += tmpy[r + half];
+          }
+        }
+        ex += tmpx[0];
+        ey += tmpy[0];
+      }
+    }
+    eff[2 * i] = ex;
+    eff[2 * i + 1] = ey;
+  }
+}
+
+/* p2m: p2mWeight (p2m.cu:24-35) forms x*m; the per-cell sums follow check/core/solver/p2m.cu:36-46
+ * (sequential in sorted order); the centre of mass is (sum x*m) / (sum m) per component (p2m.cu:72). */
+void orc_p2m(int n, int base_dim, const float* pos, const float* w, const int* head,
+             float* cell_pos, float* cell_w) {
+  const int C = base_dim * base_dim;
+  (void)n;
+  for (int c = 0; c < C; ++c) {
+    float sx = 0.0f, sy = 0.0f, sw = 0.0f;
+    for (int k = head[c]; k < head[c + 1]; ++k) {
+      sx += pos[2 * k] * w[k];
+      sy += pos[2 * k + 1] * w[k];
+      sw += w[k];
+    }
+    if (head[c] != head[c + 1]) {
+      sx = sx / sw;
+      sy = sy / sw;
+    }
+    cell_pos[2 * c] = sx;
+    cell_pos[2 * c + 1] = sy;
+    cell_w[c] = sw;
+  }
+}
+
+/* m2m.cu:22-74: parent = mass-weighted mean of its 4 children, summed left to right. */
+void orc_m2m(int num_level, int base_dim, float* cell_pos, float* cell_w) {
+  const int B = base_dim;
+  if (num_level <= 1) return;
+  for (int level = 1; level < num_level; ++level) {
+    const int cs = 1 << level;
+    const int ld = B / cs;
+    float* lp = cell_pos + 2 * (size_t)level * B * B;
+    float* lw = cell_w + (size_t)level * B * B;
+    for (int ty = 0; ty < ld; ++ty) {
+      for (int tx = 0; tx < ld; ++tx) {
+        const int idx = (tx + ty * B) * cs;
+        const int ch = idx - B * B;
+        const int ox = cs / 2;
+        const int oy = ox * B;
+        const int c[4] = {ch, ch + ox, ch + oy, ch + ox + oy};
+        float px = lp[2 * c[0]] * lw[c[0]];
+        float py = lp[2 * c[0] + 1] * lw[c[0]];
+        float ww = lw[c[0]];
+        for (int q = 1; q < 4; ++q) {
+          px = px + lp[2 * c[q]] * lw[c[q]];
+          py = py + lp[2 * c[q] + 1] * lw[c[q]];
+          ww = ww + lw[c[q]];
+        }
+        if (ww == 0.0f) {
+          lp[2 * idx] = 0.0f;
+          lp[2 * idx + 1] = 0.0f;
+        } else {
+          lp[2 * idx] = px / ww;
+          lp[2 * idx + 1] = py / ww;
+        }
+        lw[idx] = ww;
+      }
+    }
+  }
+}
+
+/* m2l.cu:24-81: sources are the 6x6 children of the parent's 3x3 neighbours minus the target's 3x3. */
+void orc_m2l(int num_level, int base_dim, const float* cell_pos, const float* cell_w, float eps, float* cell_eff) {
+  const int B = base_dim;
+  if (num_level <= 0) return;
+  for (int level = 0; level < num_level; ++level) {
+    const int cs = 1 << level;
+    const int ld = B >> level;
+    const float* lp = cell_pos + 2 * (size_t)level * B * B;
+    const float* lw = cell_w + (size_t)level * B * B;
+    float* le = cell_eff + 2 * (size_t)level * B * B;
+#pragma omp parallel for schedule(static)
+    for (int ty = 0; ty < ld; ++ty) {
+      for (int tx = 0; tx < ld; ++tx) {
+        const int px = tx & ~1, py = ty & ~1;
+        const int tidx = (tx + ty * B) * cs;
+        const float tpx = lp[2 * tidx], tpy = lp[2 * tidx + 1];
+        float ex = 0.0f, ey = 0.0f;
+        for (int y = py - 2; y < py + 4; ++y) {
+          if (y < 0 || y >= ld) continue;
+          for (int x = px - 2; x < px + 4; ++x) {
+            if (x < 0 || x >= ld) continue;
+            if (abs(x - tx) > 1 || abs(y - ty) > 1) {
+              const int idx = (x + y * B) * cs;
+              float ax, ay;
+              orc_kernel_function(tpx, tpy, lp[2 * idx], lp[2 * idx + 1], lw[idx], eps, &ax, &ay);
+              ex += ax;
+              ey += ay;
+            }
+          }
+        }
+        le[2 * tidx] = ex;
+        le[2 * tidx + 1] = ey;
+      }
+    }
+  }
+}
+
+/* l2l.cu:21-56: from level L-2 down to 0, each cell adds its parent's effect. */
+void orc_l2l(int num_level, int base_dim, float* cell_eff) {
+  const int B = base_dim;
+  if (num_level <= 1) return;
+  for (int level = num_level - 2; level >= 0; --level) {
+    const int cs = 1 << level;
+    const int ld = B / cs;
+    float* le = cell_eff + 2 * (size_t)level * B * B;
+    for (int ty = 0; ty < ld; ++ty) {
+      for (int tx = 0; tx < ld; ++tx) {
+        const int idx = (tx + ty * B) * cs;
+        const int par = ((tx & ~1) + (ty & ~1) * B) * cs + B * B;
+        le[2 * idx] += le[2 * par];
+        le[2 * idx + 1] += le[2 * par + 1];
+      }
+    }
+  }
+}
+
+/* l2p.cu:23-48 (run for every N; the reference's launch fails above N = 1,048,576). */
+void orc_l2p(int n, int base_dim, const int* index, const float* cell_eff, float* eff) {
+  for (int i = 0; i < n; ++i) {
+    const int c = index[2 * i] + index[2 * i + 1] * base_dim;
+    eff[2 * i] += cell_eff[2 * c];
+    eff[2 * i + 1] += cell_eff[2 * c + 1];
+  }
+}
+
+/* postdo.cu:22-45. */
+void orc_postdo(int n, const int* perm, const float* eff, float* eff_origin) {
+  for (int i = 0; i < n; ++i) {
+    eff_origin[2 * perm[i]] = eff[2 * i];
+    eff_origin[2 * perm[i] + 1] = eff[2 * i + 1];
+  }
+}
+
+/* solve.cu:11-27: predo, p2p, p2m, m2m, m2l, l2l, l2p, postdo. */
+int orc_solve(int n, int num_level, const float limits[4], float eps, int p2p_block,
+              const float* pos, const float* w, float* eff) {
+  if (n <= 0) return 0;
+  const int B = orc_base_dim(num_level);
+  const size_t C = (size_t)B * B;
+  const size_t levels = num_level < 2 ? 2 : (size_t)num_level;
+  int* index = (int*)malloc(sizeof(int) * 2 * (size_t)n);
+  int* perm = (int*)malloc(sizeof(int) * (size_t)n);
+  int* head = (int*)malloc(sizeof(int) * (C + 1));
+  float* ps = (float*)malloc(sizeof(float) * 2 * (size_t)n);
+  float* ws = (float*)malloc(sizeof(float) * (size_t)n);
+  float* es = (float*)malloc(sizeof(float) * 2 * (size_t)n);
+  float* cp = (float*)calloc(2 * C * levels, sizeof(float));
+  float* cw = (float*)calloc(C * levels, sizeof(float));
+  float* ce = (float*)calloc(2 * C * levels, sizeof(float));
+  if (!index || !perm || !head || !ps || !ws || !es || !cp || !cw || !ce) {
+    free(index); free(perm); free(head); free(ps); free(ws); free(es); free(cp); free(cw); free(ce);
+    return -1;
+  }
+  orc_predo(n, num_level, limits, pos, w, index, perm, head, ps, ws);
+  if (p2p_block) {
+    orc_p2p_block(n, B, ps, ws, index, head, eps, es);
+  } else {
+    orc_p2p_naive(n, B, ps, ws, index, head, eps, es);
+  }
+  if (num_level > 0) {
+    orc_p2m(n, B, ps, ws, head, cp, cw);
+    orc_m2m(num_level, B, cp, cw);
+    orc_m2l(num_level, B, cp, cw, eps, ce);
+    orc_l2l(num_level, B, ce);
+    orc_l2p(n, B, index, ce, es);
+  }
+  orc_postdo(n, perm, es, eff);
+  free(index); free(perm); free(head); free(ps); free(ws); free(es); free(cp); free(cw); free(ce);
+  return 0;
+}
+
+/* The solve restricted to a list of targets (original indices): the tree is built in full, P2P and L2P
+ * run for the listed particles only, in p2pNaive order. eff receives 2 floats per listed target. */
+int orc_solve_targets(int n, int num_level, const float limits[4], float eps, const float* pos, const float* w,
+                      const int* targets, int n_targets, float* eff) {
+  if (n <= 0) return 0;
+  const int B = orc_base_dim(num_level);
+  const size_t C = (size_t)B * B;
+  const size_t levels = num_level < 2 ? 2 : (size_t)num_level;
+  int* index = (int*)malloc(sizeof(int) * 2 * (size_t)n);
+  int* perm = (int*)malloc(sizeof(int) * (size_t)n);
+  int* inv = (int*)malloc(sizeof(int) * (size_t)n);
+  int* head = (int*)malloc(sizeof(int) * (C + 1));
+  float* ps = (float*)malloc(sizeof(float) * 2 * (size_t)n);
+  float* ws = (float*)malloc(sizeof(float) * (size_t)n);
+  float* cp = (float*)calloc(2 * C * levels, sizeof(float));
+  float* cw = (float*)calloc(C * levels, sizeof(float));
+  float* ce = (float*)calloc(2 * C * levels, sizeof(float));
+  if (!index || !perm || !inv || !head || !ps || !ws || !cp || !cw || !ce) {
+    free(index); free(perm); free(inv); free(head); free(ps); free(ws); free(cp); free(cw); free(ce);
+    return -1;
+  }
+  orc_predo(n, num_level, limits, pos, w, index, perm, head, ps, ws);
+  for (int i = 0; i < n; ++i) inv[perm[i]] = i;
+  if (num_level > 0) {
+    orc_p2m(n, B, ps, ws, head, cp, cw);
+    orc_m2m(num_level, B, cp, cw);
+    orc_m2l(num_level, B, cp, cw, eps, ce);
+    orc_l2l(num_level, B, ce);
+  }
+#pragma omp parallel for schedule(dynamic, 16)
+  for (int t = 0; t < n_targets; ++t) {
+    const int i = inv[targets[t]];
+    const int px = index[2 * i], py = index[2 * i + 1];
+    float ex = 0.0f, ey = 0.0f;
+    for (int y = py - 1; y <= py + 1; ++y) {
+      for (int x = px - 1; x <= px + 1; ++x) {
+        if (x < 0 || x >= B || y < 0 || y >= B) continue;
+        const int c = x + y * B;
+        for (int k = head[c]; k < head[c + 1]; ++k) {
+          if (k == i) continue;
+          float ax, ay;
+          orc_kernel_function(ps[2 * i], ps[2 * i + 1], ps[2 * k], ps[2 * k + 1], ws[k], eps, &ax, &ay);
+          ex += ax;
+          ey += ay;
+        }
+      }
+    }
+    if (num_level > 0) {
+      ex += ce[2 * (px + py * B)];
+      ey += ce[2 * (px + py * B) + 1];
+    }
+    eff[2 * t] = ex;
+    eff[2 * t + 1] = ey;
+  }
+  free(index); free(perm); free(inv); free(head); free(ps); free(ws); free(cp); free(cw); free(ce);
+  return 0;
+}
+
+/* update.cu:26-55 and prune.cu:28-62. The position update 2x - x_prev + a*tick*tick is evaluated as
+ * fmaf(a*tick, tick, 2x - x_prev), the multiply-add the CUDA compiler forms from update.cu:39. */
+int orc_stars_update(int n, int num_level, const float limits[4], float eps, int p2p_block, float tick_scaled,
+                     float* cur, float* prev, float* w, float* acc) {
+  if (orc_solve(n, num_level, limits, eps, p2p_block, cur, w, acc) != 0) return -1;
+  for (int i = 0; i < n; ++i) {
+    for (int d = 0; d < 2; ++d) {
+      const float p = cur[2 * i + d];
+      const float base = 2.0f * p - prev[2 * i + d];
+      cur[2 * i + d] = fmaf(acc[2 * i + d] * tick_scaled, tick_scaled, base);
+      prev[2 * i + d] = p;
+    }
+  }
+  /* prune.cu:40-41 flags, prune.cu:60 stable partition (kept stars first, order preserved). */
+  int kept = 0;
+  float* dead = (float*)malloc(sizeof(float) * 5 * (size_t)(n > 0 ? n : 1));
+  int ndead = 0;
+  for (int i = 0; i < n; ++i) {
+    const float x = cur[2 * i], y = cur[2 * i + 1];
+    const int out = (x < limits[0] || y < limits[1] || x > limits[2] || y > limits[3]);
+    if (!out) {
+      cur[2 * kept] = x;
+      cur[2 * kept + 1] = y;
+      prev[2 * kept] = prev[2 * i];
+      prev[2 * kept + 1] = prev[2 * i + 1];
+      w[kept] = w[i];
+      ++kept;
+    } else {
+      dead[5 * ndead + 0] = x;
+      dead[5 * ndead + 1] = y;
+      dead[5 * ndead + 2] = prev[2 * i];
+      dead[5 * ndead + 3] = prev[2 * i + 1];
+      dead[5 * ndead + 4] = w[i];
+      ++ndead;
+    }
+  }
+  for (int j = 0; j < ndead; ++j) {
+    const int i = kept + j;
+    cur[2 * i] = dead[5 * j + 0];
+    cur[2 * i + 1] = dead[5 * j + 1];
+    prev[2 * i] = dead[5 * j + 2];
+    prev[2 * i + 1] = dead[5 * j + 3];
+    w[i] = dead[5 * j + 4];
+  }
+  free(dead);
+  return kept;
+}
+
+/* All-pairs direct sum in FP64, the error reference for every result (demo.cu:59-66 pattern). */
+void orc_direct_f64(int n, const float* pos, const float* w, double eps, const int* targets, int n_targets,
+                    double* eff) {
+  const int nt = targets ? n_targets : n;
+#pragma omp parallel for schedule(dynamic, 16)
+  for (int t = 0; t < nt; ++t) {
+    const int i = targets ? targets[t] : t;
+    const double tx = pos[2 * i], ty = pos[2 * i + 1];
+    double ex = 0.0, ey = 0.0;
+    for (int j = 0; j < n; ++j) {
+      if (j == i) continue;
+      const double dx = (double)pos[2 * j] - tx;
+      const double dy = (double)pos[2 * j + 1] - ty;
+      const double r = sqrt(dx * dx + dy * dy);
+      const double s = (double)w[j] / (r * r * r + eps);
+      ex += dx * s;
+      ey += dy * s;
+    }
+    eff[2 * t] = ex;
+    eff[2 * t + 1] = ey;
+  }
+}
+
+long long orc_p2p_pairs(int base_dim, const int* head) {
+  const int B = base_dim;
+  long long total = 0;
+  for (int y = 0; y < B; ++y) {
+    for (int x = 0; x < B; ++x) {
+      const int c = x + y * B;
+      const long long nt = head[c + 1] - head[c];
+      if (nt == 0) continue;
+      long long ns = 0;
+      for (int yy = y - 1; yy <= y + 1; ++yy) {
+        if (yy < 0 || yy >= B) continue;
+        const int lo = x - 1 > 0 ? x - 1 : 0;
+        const int hi = x + 1 < B ? x + 1 : B - 1;
+        ns += head[hi + yy * B + 1] - head[lo + yy * B];
+      }
+      total += nt * (ns - 1);
+    }
+  }
+  return total;
+}

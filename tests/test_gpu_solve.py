@@ -1,0 +1,166 @@
+"""GPU: Solver::solve parity with the oracle (the reference's algorithm restated on the CPU).
+
+Bar: cell order bit-exact; effects within 1e-5 of the oracle under the guarded relative metric
+max_i |a_i - a_i^ref| / max(|a_i^ref|, 1e-3 * median |a^ref|). The oracle sums P2P in the reference's
+p2pNaive order (the path the reference takes above 65,535 particles); the engine sums in the same order
+with hardware sqrt/reciprocal approximations. Each case also reports its error against the FP64 direct sum.
+"""
+import numpy as np
+import pytest
+
+from conftest import guarded_rel_err
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-5
+
+
+def run_solve(engine, pos, w, num_level, limits, eps, max_n=None):
+    import torch
+
+    n = len(w)
+    s = engine.Solver(num_level, max_n or max(n, 1), limits, epsilon=eps)
+    p = torch.from_numpy(np.ascontiguousarray(pos, np.float32)).cuda()
+    m = torch.from_numpy(np.ascontiguousarray(w, np.float32)).cuda()
+    e = torch.full((max(n, 1), 2), float("nan"), device="cuda")
+    s.solve(n, p, m, e)
+    torch.cuda.synchronize()
+    out = e[:n].cpu().numpy()
+    return s, out
+
+
+def uniform(n, seed, lo=-1.0, hi=1.0):
+    rng = np.random.default_rng(seed)
+    return rng.uniform(lo, hi, (n, 2)).astype(np.float32), rng.uniform(0.5, 1.5, n).astype(np.float32)
+
+
+def test_reference_fixture_solve(engine, golden, orc):
+    pos, w = golden["position"].reshape(-1, 2), golden["weight"]
+    lim = (0.0, -1.0, 8.0, 2.0)
+    s, eff = run_solve(engine, pos, w, 3, lim, 0.1)
+    assert guarded_rel_err(eff, orc.solve(pos, w, 3, lim, 0.1))[0] < TOL
+    # the reference's own path at this size is p2pBlock (N <= 65535); its order differs by rounding only
+    assert guarded_rel_err(eff, orc.solve(pos, w, 3, lim, 0.1, block=True))[0] < 1e-4
+
+
+@pytest.mark.parametrize("n,level", [(1, 2), (2, 2), (31, 1), (1000, 0), (4095, 3), (4096, 3), (4097, 3),
+                                     (12345, 4), (16384, 3), (65536, 5)])
+def test_uniform_sizes(engine, orc, n, level):
+    pos, w = uniform(n, 100 + n)
+    lim = (-1.0, -1.0, 1.0, 1.0)
+    s, eff = run_solve(engine, pos, w, level, lim, 1e-3)
+    ref = orc.solve(pos, w, level, lim, 1e-3)
+    err, _ = guarded_rel_err(eff, ref)
+    assert err < TOL, f"guarded relative error {err:.3e}"
+
+
+def test_disk_against_oracle_and_fp64(engine, orc):
+    from nbfmm_gb300 import workloads
+
+    sysm = workloads.disk(1 << 18, seed=5, num_level=5)
+    s, eff = run_solve(engine, sysm.position, sysm.weight, sysm.num_level, sysm.limits, sysm.epsilon)
+    ref = orc.solve(sysm.position, sysm.weight, sysm.num_level, sysm.limits, sysm.epsilon)
+    err, errs = guarded_rel_err(eff, ref)
+    print(f"disk 262144: guarded max {err:.3e}, p99.9 {np.quantile(errs, 0.999):.3e}")
+    assert err < TOL
+    t = np.random.default_rng(0).choice(len(sysm.weight), 512, replace=False)
+    d = orc.direct_f64(sysm.position, sysm.weight, sysm.epsilon, t)
+    e_gpu = np.linalg.norm(eff[t] - d, axis=1) / np.linalg.norm(d, axis=1)
+    e_orc = np.linalg.norm(ref[t] - d, axis=1) / np.linalg.norm(d, axis=1)
+    print(f"vs FP64 direct sum: engine median {np.median(e_gpu):.3e}, oracle median {np.median(e_orc):.3e}")
+    assert np.median(e_gpu) <= np.median(e_orc) * 1.001 + 1e-7
+
+
+def test_zero_particles_is_a_no_op(engine):
+    import torch
+
+    s = engine.Solver(3, 16, (-1, -1, 1, 1))
+    e = torch.full((16, 2), 7.0, device="cuda")
+    s.solve(0, e, e[:, 0].contiguous(), e)
+    torch.cuda.synchronize()
+    assert torch.all(e == 7.0)
+
+
+def test_one_dense_cell_spans_many_chunks(engine, orc):
+    # 1500 particles in one leaf cell (several 256-target chunks) plus a sparse background
+    rng = np.random.default_rng(21)
+    dense = rng.uniform(0.01, 0.11, (1500, 2)).astype(np.float32)
+    sparse = rng.uniform(-1, 1, (500, 2)).astype(np.float32)
+    pos = np.concatenate([dense, sparse])
+    w = rng.uniform(0.5, 1.5, 2000).astype(np.float32)
+    lim = (-1.0, -1.0, 1.0, 1.0)
+    s, eff = run_solve(engine, pos, w, 3, lim, 1e-3)
+    assert guarded_rel_err(eff, orc.solve(pos, w, 3, lim, 1e-3))[0] < TOL
+
+
+def test_boundary_outside_and_coincident_particles(engine, orc):
+    rng = np.random.default_rng(22)
+    pos, w = uniform(3000, 22)
+    pos[:10] = [1.0, 1.0]           # on the upper limits: clamped into the last cell
+    pos[10:20, 0] = -1.0            # on the lower x limit
+    pos[20:25] = [[5.0, 0.0], [-3.0, 0.5], [0.0, 9.0], [0.2, -7.0], [2.0, 2.0]]  # outside: clamped
+    pos[25:40] = pos[40]            # coincident particles contribute zero to each other
+    lim = (-1.0, -1.0, 1.0, 1.0)
+    s, eff = run_solve(engine, pos, w, 4, lim, 1e-3)
+    ref = orc.solve(pos, w, 4, lim, 1e-3)
+    assert np.all(np.isfinite(eff))
+    assert guarded_rel_err(eff, ref)[0] < TOL
+
+
+def test_solve_smaller_than_capacity_and_repeat(engine, orc):
+    import torch
+
+    pos, w = uniform(5000, 23)
+    lim = (-1.0, -1.0, 1.0, 1.0)
+    s = engine.Solver(4, 20000, lim, epsilon=1e-3)
+    p, m = torch.from_numpy(pos).cuda(), torch.from_numpy(w).cuda()
+    e1 = torch.zeros(5000, 2, device="cuda")
+    e2 = torch.zeros(5000, 2, device="cuda")
+    s.solve(5000, p, m, e1)
+    s.solve(5000, p, m, e2)
+    torch.cuda.synchronize()
+    assert torch.equal(e1, e2)  # deterministic
+    assert guarded_rel_err(e1.cpu().numpy(), orc.solve(pos, w, 4, lim, 1e-3))[0] < TOL
+
+
+def test_invalid_count_raises(engine):
+    import torch
+
+    s = engine.Solver(3, 100, (-1, -1, 1, 1))
+    e = torch.zeros(200, 2, device="cuda")
+    with pytest.raises(engine.NbfmmError):
+        s.solve(101, e, e[:, 0].contiguous(), e)
+
+
+def test_full_size_disk_sampled_targets(engine, orc):
+    """Config 2 at full size (N = 1,048,576, depth 7): sampled targets against the oracle's restricted solve."""
+    from nbfmm_gb300 import workloads
+
+    sysm = workloads.disk(1 << 20, seed=2, num_level=6)
+    s, eff = run_solve(engine, sysm.position, sysm.weight, sysm.num_level, sysm.limits, sysm.epsilon)
+    t = np.random.default_rng(1).choice(sysm.n, 4096, replace=False)
+    ref = orc.solve_targets(sysm.position, sysm.weight, sysm.num_level, sysm.limits, sysm.epsilon, t)
+    assert guarded_rel_err(eff[t], ref)[0] < TOL
+
+
+def test_two_disks_16m_order_properties(engine):
+    """Config 3 at full size (N = 16,777,216, depth 9): size-independent checks of the preassign --
+    keys sorted, permutation valid and stable, heads consistent, every effect finite."""
+    import torch
+    from nbfmm_gb300 import workloads
+
+    sysm = workloads.two_disks(1 << 24, seed=3, num_level=8)
+    s, eff = run_solve(engine, sysm.position, sysm.weight, sysm.num_level, sysm.limits, sysm.epsilon)
+    assert np.all(np.isfinite(eff))
+    buf = s.buffers()
+    n = sysm.n
+    key = buf["cell_key"][:n]
+    perm = buf["perm"][:n]
+    assert bool(torch.all(key[1:] >= key[:-1]))
+    same = key[1:] == key[:-1]
+    assert bool(torch.all((perm[1:] > perm[:-1]) | ~same))  # stable within a cell
+    assert int(torch.bincount(perm.long(), minlength=n).max()) == 1
+    head = buf["head"]
+    assert int(head[-1]) == n and bool(torch.all(head[1:] >= head[:-1]))
+    counts = torch.bincount(key.long(), minlength=head.numel() - 1)
+    assert bool(torch.all(counts == head[1:] - head[:-1]))

@@ -1,0 +1,118 @@
+"""GPU: the Stars update path (solve + Stormer-Verlet + prune, update.cu:47-55) against the oracle stepping the
+reference's update one call at a time, including the order the reference's prune leaves the arrays in."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def make_stars(engine, cur, prev, w, level, limits, tick, eps):
+    import torch
+
+    st = engine.Stars(level, len(w), tick=tick, grav_const=1.0, position_limits=limits, epsilon=eps)
+    st.gpuptr_position_cur_[:] = torch.from_numpy(cur).cuda()
+    st.gpuptr_position_pre_[:] = torch.from_numpy(prev).cuda()
+    st.gpuptr_weight_[:] = torch.from_numpy(w).cuda()
+    return st
+
+
+def oracle_steps(orc, cur, prev, w, level, limits, tick, eps, steps):
+    n = len(w)
+    cur, prev, w = cur.copy(), prev.copy(), w.copy()
+    for _ in range(steps):
+        k, c2, p2, w2, _ = orc.stars_update(cur[:n], prev[:n], w[:n], level, limits, eps, tick)
+        cur[:n], prev[:n], w[:n] = c2, p2, w2
+        n = k
+    return n, cur, prev, w
+
+
+def system(n, seed, escape=()):
+    rng = np.random.default_rng(seed)
+    cur = rng.uniform(-0.9, 0.9, (n, 2)).astype(np.float32)
+    prev = (cur - rng.normal(0, 2e-4, (n, 2))).astype(np.float32)
+    w = (rng.uniform(0.5, 1.5, n) / n).astype(np.float32)
+    w += np.arange(n, dtype=np.float32) * np.float32(1e-9)  # distinct weights identify stars
+    for i, (idx, speed) in enumerate(escape):
+        cur[idx] = [0.85, 0.0]
+        prev[idx] = [0.85 - speed, 0.0]
+    return cur, prev, w
+
+
+def close_positions(a, b, tick, scale=1.0):
+    # differences come from effect rounding (1e-5 relative) times tick^2, plus a couple of ulps
+    tol = 4 * np.spacing(np.abs(b).astype(np.float32)) + 1e-5 * scale * tick * tick
+    return np.all(np.abs(a - b) <= tol)
+
+
+def test_one_update_matches_oracle(engine, orc):
+    import torch
+
+    cur, prev, w = system(4096, 1)
+    lim, tick, eps = (-1.0, -1.0, 1.0, 1.0), 1e-3, 1e-3
+    st = make_stars(engine, cur, prev, w, 3, lim, tick, eps)
+    st.update(1)
+    torch.cuda.synchronize()
+    n, c_ref, p_ref, w_ref = oracle_steps(orc, cur, prev, w, 3, lim, tick, eps, 1)
+    assert st.num_star_ == n
+    c = st.gpuptr_position_cur_.cpu().numpy()
+    np.testing.assert_array_equal(st.gpuptr_weight_.cpu().numpy(), w_ref)
+    np.testing.assert_array_equal(st.gpuptr_position_pre_.cpu().numpy(), p_ref)
+    acc_scale = np.abs(orc.solve(cur, w, 3, lim, eps)).max()
+    assert close_positions(c, c_ref, tick, acc_scale)
+
+
+def test_prune_order_over_several_updates(engine, orc):
+    import torch
+
+    # stars escaping after different numbers of steps; the arrays must end in the reference's order:
+    # survivors in order, then the pruned ones, most recently pruned first
+    escape = [(5, 0.2), (17, 0.2), (300, 0.07), (301, 0.02), (1000, 0.07), (2047, 0.2)]
+    cur, prev, w = system(2048, 2, escape)
+    lim, tick, eps = (-1.0, -1.0, 1.0, 1.0), 1e-3, 1e-3
+    st = make_stars(engine, cur, prev, w, 3, lim, tick, eps)
+    st.update(6)
+    torch.cuda.synchronize()
+    n, c_ref, p_ref, w_ref = oracle_steps(orc, cur, prev, w, 3, lim, tick, eps, 6)
+    assert n < 2048 - 3
+    assert st.num_star_ == n
+    np.testing.assert_array_equal(st.gpuptr_weight_.cpu().numpy(), w_ref)  # identical layout
+
+
+def test_split_calls_equal_one_call(engine):
+    import torch
+
+    escape = [(5, 0.2), (300, 0.07), (1000, 0.02)]
+    cur, prev, w = system(2048, 3, escape)
+    lim, tick, eps = (-1.0, -1.0, 1.0, 1.0), 1e-3, 1e-3
+    a = make_stars(engine, cur, prev, w, 3, lim, tick, eps)
+    b = make_stars(engine, cur, prev, w, 3, lim, tick, eps)
+    a.update(7)
+    b.update(3)
+    b.update(4)
+    torch.cuda.synchronize()
+    assert a.num_star_ == b.num_star_
+    assert torch.equal(a.gpuptr_weight_, b.gpuptr_weight_)
+    assert torch.equal(a.gpuptr_position_cur_, b.gpuptr_position_cur_)
+    assert torch.equal(a.gpuptr_position_pre_, b.gpuptr_position_pre_)
+
+
+def test_initialize_forwards_tick_and_state(engine):
+    import torch
+
+    seen = {}
+
+    def generator(n, radius, tick, cur, prev, w):
+        seen["tick"] = tick
+        ang = torch.linspace(0, 6.28, n, device="cuda")
+        cur[:, 0] = radius * torch.cos(ang)
+        cur[:, 1] = radius * torch.sin(ang)
+        prev.copy_(cur)
+        w.fill_(1.0 / n)
+
+    st = engine.Stars(3, 256, tick=2e-3, grav_const=4.0, position_limits=(-1, -1, 1, 1))
+    st.initialize(generator, 256, 0.5)
+    assert abs(seen["tick"] - 4e-3) < 1e-9  # tick * sqrt(G) (stars.cu:31)
+    st.update(2)
+    torch.cuda.synchronize()
+    assert st.num_star_ == 256
+    assert torch.all(torch.isfinite(st.gpuptr_position_cur_))
