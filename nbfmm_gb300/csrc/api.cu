@@ -487,9 +487,10 @@ struct nbfmm_stars {
     a.state4 = state4;
     a.state_prev = state_prev;
     a.tick = tick;
-    cudaEventRecord(cap_a, s);
+    // External records: captured as event record nodes (a plain record is only a capture-ordering marker).
+    cudaEventRecordWithFlags(cap_a, s, cudaEventRecordExternal);
     launch_p2p(a, kVerlet, v.num_sms, s);
-    cudaEventRecord(cap_b, s);
+    cudaEventRecordWithFlags(cap_b, s, cudaEventRecordExternal);
     launch_finish_step(sc, s);
   }
 

@@ -74,14 +74,36 @@ __device__ __forceinline__ float2 kernel_exact(float2 t, float2 s, float m, floa
   return make_float2(__fmul_rn(dx, tmp), __fmul_rn(dy, tmp));
 }
 
+// Leaf sums of x*m, y*m and m over one cell, one warp per cell. Each lane contributes the products of one
+// particle of the current 32-particle chunk; the sums are then accumulated one particle at a time in sorted
+// order (lane 0, 1, ... of each chunk), so they round exactly like the sequential loop of the reference's
+// P2M check (check/core/solver/p2m.cu:36-46). Every lane ends with the same sums.
+__device__ __forceinline__ void cell_sums_add_chunk(float& sx, float& sy, float& sw, float x, float y, float m,
+                                                    int count) {
+  const float px = __fmul_rn(x, m);
+  const float py = __fmul_rn(y, m);
+  for (int j = 0; j < count; ++j) {
+    sx = __fadd_rn(sx, __shfl_sync(0xffffffffu, px, j));
+    sy = __fadd_rn(sy, __shfl_sync(0xffffffffu, py, j));
+    sw = __fadd_rn(sw, __shfl_sync(0xffffffffu, m, j));
+  }
+}
+
+// Centre of mass (p2m.cu:72): (sum x*m) / (sum m) per component; an empty cell is (0, 0) with mass 0.
+__device__ __forceinline__ float4 centre_of_mass(float sx, float sy, float sw, bool nonempty) {
+  if (!nonempty) return make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+  return make_float4(__fdiv_rn(sx, sw), __fdiv_rn(sy, sw), sw, 0.0f);
+}
+
 // ---- launchers (defined in sort.cu / tree.cu / p2p.cu), all asynchronous on `stream` --------------------
 
 // Keys of positions given as float2 [n] (caller order); values = 0..n-1.
 void launch_keys_from_positions(const Geometry& g, const float2* pos, const int* d_n, uint32_t* keys,
                                 uint32_t* vals, int max_n, cudaStream_t stream);
 
-// Stable LSD radix sort of (keys, vals) on the low `key_bits` bits; n read from device memory.
-// Sorted output ends in (keys_a, vals_a). Returns 0, or -1 on an invalid configuration.
+// Stable LSD radix sort of (keys, vals) on the low `key_bits` bits; n read from device memory. Passes
+// alternate between the two buffer pairs; returns 0 when the result is in (keys_a, vals_a), 1 when it is in
+// (keys_b, vals_b).
 int launch_radix_sort(uint32_t* keys_a, uint32_t* vals_a, uint32_t* keys_b, uint32_t* vals_b,
                       uint32_t* counts, uint32_t* digit_total, const int* d_n, int max_n, int key_bits,
                       cudaStream_t stream);

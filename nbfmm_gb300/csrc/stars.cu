@@ -19,12 +19,6 @@ namespace nbfmm_gb300 {
 
 namespace {
 
-__device__ __forceinline__ float warp_sum(float v) {
-#pragma unroll
-  for (int d = 16; d >= 1; d >>= 1) v = __fadd_rn(v, __shfl_xor_sync(0xffffffffu, v, d));
-  return v;
-}
-
 __global__ void import_kernel(StepCounters sc, const float2* __restrict__ cur, const float2* __restrict__ prev,
                               const float* __restrict__ w, float4* __restrict__ state4,
                               float2* __restrict__ state_prev, float* __restrict__ w_by_orig) {
@@ -78,22 +72,18 @@ __global__ void gather_state_p2m_kernel(int num_cells, const int* __restrict__ h
   for (int c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; c < num_cells; c += nwarps) {
     const int h0 = head[c], h1 = head[c + 1];
     float sx = 0.0f, sy = 0.0f, sw = 0.0f;
-    for (int i = h0 + lane; i < h1; i += 32) {
-      const uint32_t p = perm[i];
-      const float4 q = state4[p];
-      sorted4[i] = q;
-      sprev[i] = state_prev[p];
-      sx = __fadd_rn(sx, __fmul_rn(q.x, q.z));
-      sy = __fadd_rn(sy, __fmul_rn(q.y, q.z));
-      sw = __fadd_rn(sw, q.z);
+    for (int base = h0; base < h1; base += 32) {
+      const int i = base + lane;
+      float4 q = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+      if (i < h1) {
+        const uint32_t p = perm[i];
+        q = state4[p];
+        sorted4[i] = q;
+        sprev[i] = state_prev[p];
+      }
+      cell_sums_add_chunk(sx, sy, sw, q.x, q.y, q.z, min(32, h1 - base));
     }
-    sx = warp_sum(sx);
-    sy = warp_sum(sy);
-    sw = warp_sum(sw);
-    if (lane == 0) {
-      cell0[c] = (h1 > h0) ? make_float4(__fdiv_rn(sx, sw), __fdiv_rn(sy, sw), sw, 0.0f)
-                           : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-    }
+    if (lane == 0) cell0[c] = centre_of_mass(sx, sy, sw, h1 > h0);
   }
 }
 

@@ -3,7 +3,7 @@
 //
 // Reference stages replaced (source/nbfmm/core/solver/):
 //   permuteInputVector  predo.cu:86-100    fused with P2M below (one pass over the sorted particles)
-//   p2m                 p2m.cu:24-110      segmented sums per leaf cell by one warp, no reduce_by_key, no host sync
+//   p2m                 p2m.cu:24-110      per-cell sums by one warp in sorted order, no reduce_by_key, no host sync
 //   m2m                 m2m.cu:22-74       one thread per parent cell, compact per-level layout
 //   m2l                 m2l.cu:24-81       16x16 target tile per CTA with its 20x20 source halo in shared memory
 //   l2l                 l2l.cu:21-56       fused into M2L on the way down (child = m2l + parent)
@@ -17,17 +17,6 @@ namespace nbfmm_gb300 {
 
 namespace {
 
-__device__ __forceinline__ float warp_sum(float v) {
-#pragma unroll
-  for (int d = 16; d >= 1; d >>= 1) v = __fadd_rn(v, __shfl_xor_sync(0xffffffffu, v, d));
-  return v;
-}
-
-__device__ __forceinline__ float4 centre_of_mass(float sx, float sy, float sw, bool nonempty) {
-  if (!nonempty) return make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-  return make_float4(__fdiv_rn(sx, sw), __fdiv_rn(sy, sw), sw, 0.0f);
-}
-
 __global__ void gather_p2m_kernel(int num_cells, const int* __restrict__ head, const uint32_t* __restrict__ perm,
                                   const float2* __restrict__ pos, const float* __restrict__ w,
                                   float4* __restrict__ sorted4, float4* __restrict__ cell0) {
@@ -36,18 +25,18 @@ __global__ void gather_p2m_kernel(int num_cells, const int* __restrict__ head, c
   for (int c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; c < num_cells; c += nwarps) {
     const int h0 = head[c], h1 = head[c + 1];
     float sx = 0.0f, sy = 0.0f, sw = 0.0f;
-    for (int i = h0 + lane; i < h1; i += 32) {
-      const uint32_t p = perm[i];
-      const float2 q = pos[p];
-      const float m = w[p];
-      sorted4[i] = make_float4(q.x, q.y, m, __int_as_float((int)p));
-      sx = __fadd_rn(sx, __fmul_rn(q.x, m));
-      sy = __fadd_rn(sy, __fmul_rn(q.y, m));
-      sw = __fadd_rn(sw, m);
+    for (int base = h0; base < h1; base += 32) {
+      const int i = base + lane;
+      float2 q = make_float2(0.0f, 0.0f);
+      float m = 0.0f;
+      if (i < h1) {
+        const uint32_t p = perm[i];
+        q = pos[p];
+        m = w[p];
+        sorted4[i] = make_float4(q.x, q.y, m, __int_as_float((int)p));
+      }
+      cell_sums_add_chunk(sx, sy, sw, q.x, q.y, m, min(32, h1 - base));
     }
-    sx = warp_sum(sx);
-    sy = warp_sum(sy);
-    sw = warp_sum(sw);
     if (lane == 0) cell0[c] = centre_of_mass(sx, sy, sw, h1 > h0);
   }
 }
@@ -59,15 +48,11 @@ __global__ void p2m_kernel(int num_cells, const int* __restrict__ head, const fl
   for (int c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; c < num_cells; c += nwarps) {
     const int h0 = head[c], h1 = head[c + 1];
     float sx = 0.0f, sy = 0.0f, sw = 0.0f;
-    for (int i = h0 + lane; i < h1; i += 32) {
-      const float4 q = sorted4[i];
-      sx = __fadd_rn(sx, __fmul_rn(q.x, q.z));
-      sy = __fadd_rn(sy, __fmul_rn(q.y, q.z));
-      sw = __fadd_rn(sw, q.z);
+    for (int base = h0; base < h1; base += 32) {
+      const int i = base + lane;
+      const float4 q = (i < h1) ? sorted4[i] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+      cell_sums_add_chunk(sx, sy, sw, q.x, q.y, q.z, min(32, h1 - base));
     }
-    sx = warp_sum(sx);
-    sy = warp_sum(sy);
-    sw = warp_sum(sw);
     if (lane == 0) cell0[c] = centre_of_mass(sx, sy, sw, h1 > h0);
   }
 }

@@ -53,3 +53,22 @@ def guarded_rel_err(a, ref):
     guard[guard == 0] = 1.0
     err = np.linalg.norm(a - ref, axis=1) / guard
     return float(err.max()) if len(err) else 0.0, err
+
+
+PARITY_TOL = 1e-5
+
+
+def assert_solve_parity(eff, pos, w, num_level, limits, eps, orc, tol=PARITY_TOL):
+    """Effects against the oracle's solve (p2pNaive order).
+
+    p99.9 of the guarded relative error must be below `tol`. Its maximum must be below `tol` or, where the
+    reference's own two P2P code paths -- p2pNaive and p2pBlock, chosen by N at p2p.cu:169 -- disagree by
+    more than that on the same input (FP32 reordering under cancellation, e.g. uniform squares), below
+    that disagreement. Returns (max, p99.9, reference disagreement)."""
+    ref = orc.solve(pos, w, num_level, limits, eps)
+    err, errs = guarded_rel_err(eff, ref)
+    noise = guarded_rel_err(orc.solve(pos, w, num_level, limits, eps, block=True), ref)[0]
+    p999 = float(np.quantile(errs, 0.999)) if len(errs) else 0.0
+    assert p999 < tol, f"p99.9 guarded relative error {p999:.3e}"
+    assert err < max(tol, noise), f"guarded relative error {err:.3e} (reference paths disagree by {noise:.3e})"
+    return err, p999, noise

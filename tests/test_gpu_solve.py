@@ -1,14 +1,15 @@
 """GPU: Solver::solve parity with the oracle (the reference's algorithm restated on the CPU).
 
-Bar: cell order bit-exact; effects within 1e-5 of the oracle under the guarded relative metric
-max_i |a_i - a_i^ref| / max(|a_i^ref|, 1e-3 * median |a^ref|). The oracle sums P2P in the reference's
-p2pNaive order (the path the reference takes above 65,535 particles); the engine sums in the same order
-with hardware sqrt/reciprocal approximations. Each case also reports its error against the FP64 direct sum.
+Bar: cell order bit-exact; the far field (every cell centre of mass, mass and local effect) bit-exact; effects
+within 1e-5 of the oracle under the guarded relative metric max_i |a_i - a_i^ref| / max(|a_i^ref|,
+1e-3 * median |a^ref|) -- see conftest.assert_solve_parity for the exact rule. The oracle sums P2P in the
+reference's p2pNaive order (the path the reference takes above 65,535 particles); the engine sums in the
+same order with hardware sqrt/reciprocal approximations and fused multiply-adds.
 """
 import numpy as np
 import pytest
 
-from conftest import guarded_rel_err
+from conftest import assert_solve_parity, guarded_rel_err
 
 pytestmark = pytest.mark.gpu
 
@@ -49,9 +50,7 @@ def test_uniform_sizes(engine, orc, n, level):
     pos, w = uniform(n, 100 + n)
     lim = (-1.0, -1.0, 1.0, 1.0)
     s, eff = run_solve(engine, pos, w, level, lim, 1e-3)
-    ref = orc.solve(pos, w, level, lim, 1e-3)
-    err, _ = guarded_rel_err(eff, ref)
-    assert err < TOL, f"guarded relative error {err:.3e}"
+    assert_solve_parity(eff, pos, w, level, lim, 1e-3, orc)
 
 
 def test_disk_against_oracle_and_fp64(engine, orc):
@@ -90,7 +89,7 @@ def test_one_dense_cell_spans_many_chunks(engine, orc):
     w = rng.uniform(0.5, 1.5, 2000).astype(np.float32)
     lim = (-1.0, -1.0, 1.0, 1.0)
     s, eff = run_solve(engine, pos, w, 3, lim, 1e-3)
-    assert guarded_rel_err(eff, orc.solve(pos, w, 3, lim, 1e-3))[0] < TOL
+    assert_solve_parity(eff, pos, w, 3, lim, 1e-3, orc)
 
 
 def test_boundary_outside_and_coincident_particles(engine, orc):
@@ -102,9 +101,8 @@ def test_boundary_outside_and_coincident_particles(engine, orc):
     pos[25:40] = pos[40]            # coincident particles contribute zero to each other
     lim = (-1.0, -1.0, 1.0, 1.0)
     s, eff = run_solve(engine, pos, w, 4, lim, 1e-3)
-    ref = orc.solve(pos, w, 4, lim, 1e-3)
     assert np.all(np.isfinite(eff))
-    assert guarded_rel_err(eff, ref)[0] < TOL
+    assert_solve_parity(eff, pos, w, 4, lim, 1e-3, orc)
 
 
 def test_solve_smaller_than_capacity_and_repeat(engine, orc):
@@ -120,7 +118,7 @@ def test_solve_smaller_than_capacity_and_repeat(engine, orc):
     s.solve(5000, p, m, e2)
     torch.cuda.synchronize()
     assert torch.equal(e1, e2)  # deterministic
-    assert guarded_rel_err(e1.cpu().numpy(), orc.solve(pos, w, 4, lim, 1e-3))[0] < TOL
+    assert_solve_parity(e1.cpu().numpy(), pos, w, 4, lim, 1e-3, orc)
 
 
 def test_invalid_count_raises(engine):
@@ -164,3 +162,28 @@ def test_two_disks_16m_order_properties(engine):
     assert int(head[-1]) == n and bool(torch.all(head[1:] >= head[:-1]))
     counts = torch.bincount(key.long(), minlength=head.numel() - 1)
     assert bool(torch.all(counts == head[1:] - head[:-1]))
+
+
+def test_far_field_of_a_solve_is_bit_exact(engine, orc):
+    """Leaf sums in sorted order, M2M, M2L and L2L round exactly like the oracle: every cell centre of mass,
+    mass and local effect of a full solve equals the oracle's bit for bit."""
+    import torch
+
+    from test_gpu_stages import cube_to_compact
+
+    pos, w = uniform(20000, 31)
+    level, lim = 5, (-1.0, -1.0, 1.0, 1.0)
+    s, _ = run_solve(engine, pos, w, level, lim, 1e-3)
+    buf = s.buffers()
+    B = 1 << (level + 1)
+    r = orc.predo(pos, w, level, lim)
+    cp = np.zeros((level, B, B, 2), np.float32)
+    cw = np.zeros((level, B, B), np.float32)
+    p0, w0 = orc.p2m(r["position"], r["weight"], r["head"], B)
+    cp[0], cw[0] = p0.reshape(B, B, 2), w0.reshape(B, B)
+    cp, cw = orc.m2m(cp.reshape(-1), cw.reshape(-1), level, B)
+    ce = orc.l2l(orc.m2l(cp, cw, level, B, 1e-3), level, B)
+    cp, cw, ce = cp.reshape(level, B, B, 2), cw.reshape(level, B, B), ce.reshape(level, B, B, 2)
+    ref_cells = cube_to_compact(cp, cw, buf)
+    np.testing.assert_array_equal(buf["cell"].cpu().numpy()[:, 0:3], ref_cells[:, 0:3])
+    np.testing.assert_array_equal(buf["cell_effect"].cpu().numpy(), cube_to_compact(ce, None, buf)[:, 0:2])

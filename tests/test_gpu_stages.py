@@ -197,3 +197,16 @@ def test_cell_stages_match_oracle_bit_exact(solver, golden, orc):
     np.testing.assert_array_equal(buf["cell"].cpu().numpy()[:, 0:3], ref_cells[:, 0:3])
     re = orc.m2l(rp, rw, L, B, 0.1)
     np.testing.assert_array_equal(buf["cell_effect"].cpu().numpy(), cube_to_compact(cube(re), None, buf)[:, 0:2])
+
+
+def test_p2m_bit_exact_with_sequential_sums(solver, golden, orc):
+    """Leaf sums are accumulated one particle at a time in sorted order, like check/core/solver/p2m.cu:36-46."""
+    import torch
+
+    buf = _load_particles(solver, golden)
+    solver.p2m(N)
+    torch.cuda.synchronize()
+    c0 = compact_level(buf["cell"].cpu().numpy(), buf, 0).reshape(-1, 4)
+    cp, cw = orc.p2m(golden["position"].reshape(-1, 2), golden["weight"], golden["head"], B)
+    np.testing.assert_array_equal(c0[:, 0:2], cp)
+    np.testing.assert_array_equal(c0[:, 2], cw)
