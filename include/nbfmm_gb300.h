@@ -118,6 +118,19 @@ int nbfmm_stars_num_star(nbfmm_stars* stars, int* num_star);
  * Runs without host synchronisation; the steps are replayed from a captured CUDA graph. */
 int nbfmm_stars_update(nbfmm_stars* stars, int num_steps, void* stream);
 
+/* ---- Allocation-free cell sort ---------------------------------------------------------------------- */
+
+/* No counterpart in the reference. The leaf-cell sort of predo (cell keys, stable sort, heads) for callers
+ * that cannot allocate device memory: a plugin whose host application owns every device buffer, or code
+ * that must not trigger cudaMalloc's device synchronisation. It allocates nothing; its scratch is a fixed
+ * device array inside the library (about 4.1 MB per GPU that loads it, held until exit), so at most 262,144
+ * particles per call, and calls that overlap on the GPU race on that shared scratch. The first call on each
+ * device looks up the scratch address (cudaGetSymbolAddress) and should come before any stream capture.
+ * Outputs: gpuptr_perm [num_particle] = original index of each sorted particle (the reference's
+ * gpuptr_perm_), gpuptr_head [base_dim^2 + 1] = first sorted index of each leaf cell (gpuptr_head_). */
+int nbfmm_sort_cells_noalloc(int num_level, const float position_limits[4], int num_particle,
+                             const float* gpuptr_position, int* gpuptr_perm, int* gpuptr_head, void* stream);
+
 /* ---- Instrumentation (engine-only; the reference has no timing, no events, no counters) ------------ */
 
 /* Times the P2P launch of each of the next `max_steps` update steps with a pair of CUDA events recorded

@@ -39,6 +39,7 @@ SIGNATURES = {
     "nbfmm_stars_state": (ctypes.c_int, [_vp, ctypes.POINTER(_vp), ctypes.POINTER(_vp), ctypes.POINTER(_vp)]),
     "nbfmm_stars_num_star": (ctypes.c_int, [_vp, _c_int_p]),
     "nbfmm_stars_update": (ctypes.c_int, [_vp, ctypes.c_int, _vp]),
+    "nbfmm_sort_cells_noalloc": (ctypes.c_int, [ctypes.c_int, _c_float_p, ctypes.c_int, _vp, _vp, _vp, _vp]),
     "nbfmm_stars_profile_begin": (ctypes.c_int, [_vp, ctypes.c_int]),
     "nbfmm_stars_profile_end": (ctypes.c_int, [_vp, _c_float_p, _c_int_p]),
     "nbfmm_stars_kernel_launches": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.POINTER(ctypes.c_longlong)]),

@@ -75,6 +75,19 @@ bool limits_ok(const float* l) {
 
 }  // namespace
 
+// Sets the calling thread's last-error message from another translation unit of the library.
+namespace nbfmm_gb300 {
+int api_fail(int code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  std::vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  g_last_error = buf;
+  return code;
+}
+}  // namespace nbfmm_gb300
+
 // ---- Solver --------------------------------------------------------------------------------------------
 
 struct nbfmm_solver {
