@@ -241,6 +241,7 @@ def main():
     targets = torch.randperm(n, generator=g)[:512].cuda()
     err64 = fp64_error(torch, pos, w, eff, sysm.epsilon, targets)
     del eff
+    torch.cuda.empty_cache()  # return the FP64 check's temporaries
 
     stars = nbfmm_gb300.Stars(sysm.num_level, n, tick=sysm.dt, grav_const=sysm.grav_const,
                               position_limits=sysm.limits, epsilon=sysm.epsilon)

@@ -10,7 +10,7 @@
 //     cell4    float4 [cells]   centre of mass x, y, mass, 0
 //     ceff     float2 [cells]   local (far-field) effect
 //   head     int32 [B*B + 1]  first sorted index of each leaf cell
-//   work     int2  [...]      non-empty (cell, target chunk) items for P2P
+//   work     int2  [...]      non-empty (cell, chunk of up to 128 targets) items for P2P
 // B = 2^(num_level + 1) leaf cells per side (source/nbfmm/core/solver.cu:19).
 #pragma once
 
@@ -24,10 +24,9 @@ constexpr int kSortThreads = 256;        // radix sort CTA
 constexpr int kSortItems = 16;           // items per thread
 constexpr int kSortTile = kSortThreads * kSortItems;  // 4096 items per tile
 constexpr int kRadixMaxBits = 8;
-constexpr int kP2PThreads = 128;
-constexpr int kP2PTargetsPerThread = 2;
-constexpr int kP2PChunk = kP2PThreads * kP2PTargetsPerThread;  // targets per work item
-constexpr int kP2PTile = 512;            // source particles per shared-memory tile
+constexpr int kP2PThreads = 128;        // 4 independent warps per CTA
+constexpr int kP2PPasses = 4;            // targets per lane in one work item (4 passes of 32)
+constexpr int kP2PChunk = 32 * kP2PPasses;  // targets per work item
 
 struct Geometry {
   float xmin, ymin, xmax, ymax;  // position limits [x_min, y_min, x_max, y_max]

@@ -96,4 +96,6 @@ CONFIGS = {
     "plain_16k": lambda: plain(16384, 1, 3),
     "disk_1m": lambda: disk(1 << 20, 2, 6),
     "two_disks_16m": lambda: two_disks(1 << 24, 3, 8),
+    # a quarter of the particles on a quarter of the leaf cells: the same particles per cell as two_disks_16m
+    "two_disks_4m": lambda: two_disks(1 << 22, 3, 7),
 }
