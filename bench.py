@@ -25,6 +25,10 @@ if ROOT not in sys.path:
 FLOP_PER_PAIR = 15  # 2 sub, 3 for r^2, 1 sqrt, 1 for r*r^2 (+eps fused: 2), 1 rcp, 1 mul by m, 4 for 2 FMAs
 SMS, FP32_LANES, MUFU_LANES = 152, 128, 16
 WINDOW_CELLS = 32  # side of the CPU sample window, in leaf cells
+# DRAM bytes (read + write) of one P2P launch per particle, from the ncu capture of the two-disk workload at
+# N = 4,194,304 (profiles/p2p_kernel_two_disks.md: 131.65 MB + 73.63 MB); traffic grows with the particles
+# of a launch (it equals the algorithmic 48 B/particle), so a full launch is this times N.
+P2P_DRAM_BYTES_PER_PARTICLE = (131.654144e6 + 73.634304e6) / 4194304
 
 
 def parse():
@@ -196,9 +200,78 @@ def fp64_error(torch, pos, w, eff, eps, targets):
             "targets": int(len(targets))}
 
 
+def run_batched(args):
+    """The batched form against looped single-system updates on the same systems and depths."""
+    import torch
+
+    import nbfmm_gb300
+    from nbfmm_gb300 import autotune, workloads
+
+    sysb = workloads.batched()
+    levels, report = autotune.tune_levels(nbfmm_gb300, sysb)
+    prev = sysb.previous()
+    n = sysb.n
+    b = nbfmm_gb300.Batch(sysb.offsets, levels, sysb.limits, tick=sysb.dt, grav_const=sysb.grav_const,
+                          epsilon=sysb.epsilon)
+    b.position_cur[:] = torch.from_numpy(sysb.position).cuda()
+    b.position_pre[:] = torch.from_numpy(prev).cuda()
+    b.weight[:] = torch.from_numpy(sysb.weight).cuda()
+    b.update(args.warmup)
+    torch.cuda.synchronize()
+    b.profile_begin(args.steps)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    clocks = ClockSampler("0")
+    e0.record()
+    b.update(args.steps)
+    e1.record()
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    batched_ms = e0.elapsed_time(e1)
+    p2p_ms, p2p_k = b.profile_end()
+    launches = b.kernel_launches(args.steps)
+    b.close()
+
+    stars = []
+    for s in range(sysb.num_systems):
+        lo, hi = int(sysb.offsets[s]), int(sysb.offsets[s + 1])
+        st = nbfmm_gb300.Stars(int(levels[s]), hi - lo, tick=sysb.dt, grav_const=sysb.grav_const,
+                               position_limits=tuple(float(v) for v in sysb.limits[s]), epsilon=sysb.epsilon)
+        st.gpuptr_position_cur_[:] = torch.from_numpy(sysb.position[lo:hi]).cuda()
+        st.gpuptr_position_pre_[:] = torch.from_numpy(prev[lo:hi]).cuda()
+        st.gpuptr_weight_[:] = torch.from_numpy(sysb.weight[lo:hi]).cuda()
+        st.update(args.warmup)
+        stars.append(st)
+    torch.cuda.synchronize()
+    e0.record()
+    for st in stars:
+        st.update(args.steps)
+    e1.record()
+    torch.cuda.synchronize()
+    looped_ms = e0.elapsed_time(e1)
+    value = n * args.steps / (batched_ms / 1e3)
+    looped = n * args.steps / (looped_ms / 1e3)
+    out = {
+        "metric": "particle-steps/s", "value": value, "unit": "particle-steps/s", "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": batched_ms / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded; nbfmm_gb300/workloads.py batched)",
+        "config": {"workload": f"batched: {sysb.num_systems} systems, N lognormal(median 20k, sd 0.8) clipped to "
+                               f"[2k, 262k], {n:,} particles, squares and disks, eps {sysb.epsilon:g}, "
+                               f"dt {sysb.dt:g}", "autotune": report},
+        "looped": {"value": looped, "ms_per_step": looped_ms / args.steps,
+                   "how": "one Stars per system with the same depths; update(K) per system, one after another"},
+        "speedup_vs_looped": value / looped,
+        "p2p_share_of_step": p2p_ms / batched_ms, "gpu_launches": launches, "clocks": clk,
+    }
+    print(json.dumps(out), flush=True)
+
+
 def main():
     args = parse()
     from nbfmm_gb300 import workloads
+
+    if args.config == "batched_512" and args.impl == "gb300":
+        return run_batched(args)
 
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -343,7 +416,10 @@ def main():
         "roofline": {
             "kernel": "p2p_kernel<kVerlet> (near field + L2P + Verlet epilogue)",
             "bound": "fp32", "unit": "TFLOP/s",
-            "achieved": achieved, "peak": fp32_peak, "frac": achieved / fp32_peak, "traffic": None,
+            "achieved": achieved, "peak": fp32_peak, "frac": achieved / fp32_peak,
+            "traffic": P2P_DRAM_BYTES_PER_PARTICLE * n,
+            "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of the N=4,194,304 capture, "
+                              "scaled by particles per launch",
             "peak_source": f"nominal FP32 FMA rate {SMS} SMs x {FP32_LANES} lanes x 2 at the median sampled SM clock "
                            f"({sm_mhz:.0f} MHz); MEASURED_PEAKS.json has no SIMT FP32 figure",
             "flop_per_pair": FLOP_PER_PAIR, "pairs_per_launch": pairs, "p2p_ms_per_launch": p2p_s * 1e3,

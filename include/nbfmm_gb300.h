@@ -118,6 +118,30 @@ int nbfmm_stars_num_star(nbfmm_stars* stars, int* num_star);
  * Runs without host synchronisation; the steps are replayed from a captured CUDA graph. */
 int nbfmm_stars_update(nbfmm_stars* stars, int num_steps, void* stream);
 
+/* ---- Batched form ----------------------------------------------------------------------------------- */
+
+/* No counterpart in the reference (it steps one system per Stars). Many independent systems stepped together:
+ * system s owns particles [particle_offsets[s], particle_offsets[s+1]) of the state arrays, its own limits
+ * (position_limits[4s..4s+3]) and tree depth (num_levels[s]); every step of every system is one reference
+ * Stars::update of that system alone (solve, Stormer-Verlet, prune). All systems share one sort and one
+ * P2P launch per step, and one launch per tree level; a step is replayed from a captured CUDA graph.
+ * Tables are host arrays; tick and grav_const are shared (effective tick = tick * sqrt(grav_const)). */
+typedef struct nbfmm_batch nbfmm_batch;
+int nbfmm_batch_create(int num_systems, const int* particle_offsets, const int* num_levels,
+                       const float* position_limits, float tick, float grav_const, nbfmm_batch** out);
+int nbfmm_batch_destroy(nbfmm_batch* batch);
+int nbfmm_batch_set_epsilon(nbfmm_batch* batch, float epsilon);
+/* Device state arrays over all systems (float2 / float2 / float [particle_offsets[num_systems]]). */
+int nbfmm_batch_state(nbfmm_batch* batch, float** gpuptr_position_cur, float** gpuptr_position_pre,
+                      float** gpuptr_weight);
+/* Stars left in each system (host array of num_systems); synchronises. After an update each system's range
+ * holds its survivors first, in order, then its pruned stars, most recently pruned first. */
+int nbfmm_batch_num_stars(nbfmm_batch* batch, int* num_stars);
+int nbfmm_batch_update(nbfmm_batch* batch, int num_steps, void* stream);
+int nbfmm_batch_profile_begin(nbfmm_batch* batch, int max_steps);
+int nbfmm_batch_profile_end(nbfmm_batch* batch, float* p2p_ms_total, int* p2p_launches);
+int nbfmm_batch_kernel_launches(nbfmm_batch* batch, int num_steps, long long* launches);
+
 /* ---- Allocation-free cell sort ---------------------------------------------------------------------- */
 
 /* No counterpart in the reference. The leaf-cell sort of predo (cell keys, stable sort, heads) for callers

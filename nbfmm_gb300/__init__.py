@@ -17,7 +17,7 @@ import ctypes
 
 from . import _lib
 
-__all__ = ["NbfmmError", "Solver", "Stars", "load_library"]
+__all__ = ["NbfmmError", "Solver", "Stars", "Batch", "load_library"]
 
 
 class NbfmmError(RuntimeError):
@@ -265,4 +265,85 @@ class Stars:
         """Engine kernels one update(num_steps) call launches."""
         out = ctypes.c_longlong()
         _check(_lib.load().nbfmm_stars_kernel_launches(self._h, int(num_steps), ctypes.byref(out)))
+        return int(out.value)
+
+
+class Batch:
+    """Many independent systems stepped together (the batched form; no counterpart in the reference).
+
+    System s owns particles [particle_offsets[s], particle_offsets[s+1]) of the shared state arrays, its own
+    `position_limits[s]` = (x_min, y_min, x_max, y_max) and tree depth `num_levels[s]`. Each update step of
+    each system is one Stars::update of that system alone.
+    """
+
+    def __init__(self, particle_offsets, num_levels, position_limits, tick, grav_const=1.0, epsilon: float = 0.1):
+        import numpy as np
+
+        off = np.ascontiguousarray(particle_offsets, dtype=np.int32)
+        lev = np.ascontiguousarray(num_levels, dtype=np.int32)
+        lim = np.ascontiguousarray(position_limits, dtype=np.float32).reshape(-1)
+        self.num_systems = int(len(lev))
+        if len(off) != self.num_systems + 1 or len(lim) != 4 * self.num_systems:
+            raise ValueError("need num_systems+1 offsets and 4 limits per system")
+        lib = _lib.load()
+        h = ctypes.c_void_p()
+        _check(lib.nbfmm_batch_create(self.num_systems, off.ctypes.data_as(ctypes.POINTER(ctypes.c_int)),
+                                      lev.ctypes.data_as(ctypes.POINTER(ctypes.c_int)),
+                                      lim.ctypes.data_as(ctypes.POINTER(ctypes.c_float)), float(tick),
+                                      float(grav_const), ctypes.byref(h)))
+        self._h = h
+        self.particle_offsets = off.tolist()
+        self.num_particles = int(off[-1])
+        self.set_epsilon(epsilon)
+        cur, pre, w = ctypes.c_void_p(), ctypes.c_void_p(), ctypes.c_void_p()
+        _check(lib.nbfmm_batch_state(self._h, ctypes.byref(cur), ctypes.byref(pre), ctypes.byref(w)))
+        self._ptrs = (cur.value, pre.value, w.value)
+
+    def close(self):
+        if getattr(self, "_h", None) is not None and self._h.value:
+            _lib.load().nbfmm_batch_destroy(self._h)
+        self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_epsilon(self, epsilon: float):
+        _check(_lib.load().nbfmm_batch_set_epsilon(self._h, float(epsilon)))
+        self.epsilon = float(epsilon)
+
+    @property
+    def position_cur(self):
+        return _as_tensor(self._ptrs[0], (max(self.num_particles, 1), 2), "<f4")[: self.num_particles]
+
+    @property
+    def position_pre(self):
+        return _as_tensor(self._ptrs[1], (max(self.num_particles, 1), 2), "<f4")[: self.num_particles]
+
+    @property
+    def weight(self):
+        return _as_tensor(self._ptrs[2], (max(self.num_particles, 1),), "<f4")[: self.num_particles]
+
+    @property
+    def num_stars(self):
+        out = (ctypes.c_int * self.num_systems)()
+        _check(_lib.load().nbfmm_batch_num_stars(self._h, out))
+        return list(out)
+
+    def update(self, num_steps: int = 1, stream=None):
+        _check(_lib.load().nbfmm_batch_update(self._h, int(num_steps), _stream(stream)))
+
+    def profile_begin(self, max_steps: int):
+        _check(_lib.load().nbfmm_batch_profile_begin(self._h, int(max_steps)))
+
+    def profile_end(self):
+        ms, k = ctypes.c_float(), ctypes.c_int()
+        _check(_lib.load().nbfmm_batch_profile_end(self._h, ctypes.byref(ms), ctypes.byref(k)))
+        return float(ms.value), int(k.value)
+
+    def kernel_launches(self, num_steps: int) -> int:
+        out = ctypes.c_longlong()
+        _check(_lib.load().nbfmm_batch_kernel_launches(self._h, int(num_steps), ctypes.byref(out)))
         return int(out.value)

@@ -39,6 +39,16 @@ SIGNATURES = {
     "nbfmm_stars_state": (ctypes.c_int, [_vp, ctypes.POINTER(_vp), ctypes.POINTER(_vp), ctypes.POINTER(_vp)]),
     "nbfmm_stars_num_star": (ctypes.c_int, [_vp, _c_int_p]),
     "nbfmm_stars_update": (ctypes.c_int, [_vp, ctypes.c_int, _vp]),
+    "nbfmm_batch_create": (ctypes.c_int, [ctypes.c_int, _c_int_p, _c_int_p, _c_float_p, ctypes.c_float,
+                                          ctypes.c_float, ctypes.POINTER(_vp)]),
+    "nbfmm_batch_destroy": (ctypes.c_int, [_vp]),
+    "nbfmm_batch_set_epsilon": (ctypes.c_int, [_vp, ctypes.c_float]),
+    "nbfmm_batch_state": (ctypes.c_int, [_vp, ctypes.POINTER(_vp), ctypes.POINTER(_vp), ctypes.POINTER(_vp)]),
+    "nbfmm_batch_num_stars": (ctypes.c_int, [_vp, _c_int_p]),
+    "nbfmm_batch_update": (ctypes.c_int, [_vp, ctypes.c_int, _vp]),
+    "nbfmm_batch_profile_begin": (ctypes.c_int, [_vp, ctypes.c_int]),
+    "nbfmm_batch_profile_end": (ctypes.c_int, [_vp, _c_float_p, _c_int_p]),
+    "nbfmm_batch_kernel_launches": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.POINTER(ctypes.c_longlong)]),
     "nbfmm_sort_cells_noalloc": (ctypes.c_int, [ctypes.c_int, _c_float_p, ctypes.c_int, _vp, _vp, _vp, _vp]),
     "nbfmm_stars_profile_begin": (ctypes.c_int, [_vp, ctypes.c_int]),
     "nbfmm_stars_profile_end": (ctypes.c_int, [_vp, _c_float_p, _c_int_p]),

@@ -94,6 +94,51 @@ __device__ __forceinline__ float4 centre_of_mass(float sx, float sy, float sw, b
   return make_float4(__fdiv_rn(sx, sw), __fdiv_rn(sy, sw), sw, 0.0f);
 }
 
+constexpr int kM2LTile = 16;
+constexpr int kM2LHalo = kM2LTile + 4;
+
+// M2L (m2l.cu:24-60) for one 16x16 tile of target cells of one level (x0, y0 even): the 20x20 halo of
+// sources is staged in shared memory; each target sums the children of its parent's neighbours minus its own
+// 3x3 (y outer, x inner, the reference's order) and, with add_parent, adds its parent's effect afterwards
+// (l2l.cu:33-35). `cells`/`eff` point at the level, `parent_eff` at the parent level. Called by all threads of
+// a 16x16 CTA.
+__device__ __forceinline__ void m2l_tile(float4 (*halo)[kM2LHalo], const float4* __restrict__ cells,
+                                         float2* __restrict__ eff, int dim, const float2* __restrict__ parent_eff,
+                                         int dim_parent, int add_parent, int x0, int y0, float eps) {
+  const int tid = threadIdx.y * kM2LTile + threadIdx.x;
+  for (int k = tid; k < kM2LHalo * kM2LHalo; k += kM2LTile * kM2LTile) {
+    const int hx = k % kM2LHalo, hy = k / kM2LHalo;
+    const int gx = x0 - 2 + hx, gy = y0 - 2 + hy;
+    halo[hy][hx] = (gx >= 0 && gx < dim && gy >= 0 && gy < dim) ? cells[gy * dim + gx]
+                                                                 : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+  }
+  __syncthreads();
+  const int tx = x0 + threadIdx.x, ty = y0 + threadIdx.y;
+  if (tx >= dim || ty >= dim) return;
+  const float4 t = halo[ty - y0 + 2][tx - x0 + 2];
+  const float2 tp = make_float2(t.x, t.y);
+  const int px = tx & ~1, py = ty & ~1;
+  float ex = 0.0f, ey = 0.0f;
+  for (int y = py - 2; y < py + 4; ++y) {
+    if (y < 0 || y >= dim) continue;
+    for (int x = px - 2; x < px + 4; ++x) {
+      if (x < 0 || x >= dim) continue;
+      if (abs(x - tx) > 1 || abs(y - ty) > 1) {
+        const float4 s = halo[y - y0 + 2][x - x0 + 2];
+        const float2 k = kernel_exact(tp, make_float2(s.x, s.y), s.z, eps);
+        ex = __fadd_rn(ex, k.x);
+        ey = __fadd_rn(ey, k.y);
+      }
+    }
+  }
+  if (add_parent) {
+    const float2 p = parent_eff[(ty >> 1) * dim_parent + (tx >> 1)];
+    ex = __fadd_rn(ex, p.x);
+    ey = __fadd_rn(ey, p.y);
+  }
+  eff[ty * dim + tx] = make_float2(ex, ey);
+}
+
 // ---- launchers (defined in sort.cu / tree.cu / p2p.cu), all asynchronous on `stream` --------------------
 
 // Keys of positions given as float2 [n] (caller order); values = 0..n-1.
@@ -158,6 +203,10 @@ struct P2PArgs {
   float4* state4;          // kVerlet: new state (x', y', m, original index)
   float2* state_prev;      // kVerlet: new previous positions
   float tick;              // kVerlet: tick * sqrt(G)
+  // Several systems in one global leaf-cell space (batched form); num_systems == 0 for a single system.
+  int num_systems;
+  const int* sys_cell_base;  // [num_systems + 1] first global leaf cell of each system
+  const int* sys_dim;        // [num_systems] leaf cells per side of each system
 };
 
 void launch_p2p(const P2PArgs& a, P2PEpilogue mode, int num_sms, cudaStream_t stream);

@@ -163,6 +163,13 @@ void launch_gather_state_p2m(const Geometry& g, const int* head, const uint32_t*
       cells, head, perm, state4, state_prev, sorted4, sprev, cell0);
 }
 
+void launch_gather_state_p2m_cells(const int* head, int num_cells, const uint32_t* perm, const float4* state4,
+                                   const float2* state_prev, float4* sorted4, float2* sprev, float4* cell0,
+                                   cudaStream_t stream) {
+  gather_state_p2m_kernel<<<grid_for((long long)num_cells * 32, 256, 152 * 16), 256, 0, stream>>>(
+      num_cells, head, perm, state4, state_prev, sorted4, sprev, cell0);
+}
+
 void launch_finish_step(const StepCounters& sc, cudaStream_t stream) { finish_step_kernel<<<1, 1, 0, stream>>>(sc); }
 
 void launch_export_fate(const Geometry& g, const StepCounters& sc, const float4* state4, const float2* state_prev,

@@ -25,6 +25,10 @@ void launch_keys_from_state(const Geometry& g, const StepCounters& sc, const flo
 void launch_gather_state_p2m(const Geometry& g, const int* head, const uint32_t* perm, const float4* state4,
                              const float2* state_prev, float4* sorted4, float2* sprev, float4* cell0,
                              cudaStream_t stream);
+// Same as launch_gather_state_p2m over `num_cells` leaf cells of any layout (the batched form's global space).
+void launch_gather_state_p2m_cells(const int* head, int num_cells, const uint32_t* perm, const float4* state4,
+                                   const float2* state_prev, float4* sorted4, float2* sprev, float4* cell0,
+                                   cudaStream_t stream);
 void launch_finish_step(const StepCounters& sc, cudaStream_t stream);
 void launch_export_fate(const Geometry& g, const StepCounters& sc, const float4* state4, const float2* state_prev,
                         float2* grave_cur, float2* grave_prev, int* fate, int max_n, cudaStream_t stream);

@@ -82,9 +82,6 @@ __global__ void m2m_kernel(float4* __restrict__ cell4, int off_c, int dim_c, int
   }
 }
 
-constexpr int kM2LTile = 16;
-constexpr int kM2LHalo = kM2LTile + 4;
-
 // m2l.cu:24-60 for one level. Each CTA owns a 16x16 tile of target cells (tile origin even, so the
 // children of the parents' neighbours lie in the 20x20 halo around it). With add_parent the parent's
 // effect is added afterwards (l2l.cu:33-35): child = m2l + parent.
@@ -92,39 +89,8 @@ __global__ void __launch_bounds__(kM2LTile * kM2LTile)
 m2l_kernel(const float4* __restrict__ cell4, float2* __restrict__ ceff, int off, int dim, int off_parent,
            int dim_parent, int add_parent, float eps) {
   __shared__ float4 halo[kM2LHalo][kM2LHalo];
-  const int x0 = blockIdx.x * kM2LTile, y0 = blockIdx.y * kM2LTile;
-  const int tid = threadIdx.y * kM2LTile + threadIdx.x;
-  for (int k = tid; k < kM2LHalo * kM2LHalo; k += kM2LTile * kM2LTile) {
-    const int hx = k % kM2LHalo, hy = k / kM2LHalo;
-    const int gx = x0 - 2 + hx, gy = y0 - 2 + hy;
-    halo[hy][hx] = (gx >= 0 && gx < dim && gy >= 0 && gy < dim) ? cell4[off + gy * dim + gx]
-                                                                 : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-  }
-  __syncthreads();
-  const int tx = x0 + threadIdx.x, ty = y0 + threadIdx.y;
-  if (tx >= dim || ty >= dim) return;
-  const float4 t = halo[ty - y0 + 2][tx - x0 + 2];
-  const float2 tp = make_float2(t.x, t.y);
-  const int px = tx & ~1, py = ty & ~1;
-  float ex = 0.0f, ey = 0.0f;
-  for (int y = py - 2; y < py + 4; ++y) {
-    if (y < 0 || y >= dim) continue;
-    for (int x = px - 2; x < px + 4; ++x) {
-      if (x < 0 || x >= dim) continue;
-      if (abs(x - tx) > 1 || abs(y - ty) > 1) {
-        const float4 s = halo[y - y0 + 2][x - x0 + 2];
-        const float2 k = kernel_exact(tp, make_float2(s.x, s.y), s.z, eps);
-        ex = __fadd_rn(ex, k.x);
-        ey = __fadd_rn(ey, k.y);
-      }
-    }
-  }
-  if (add_parent) {
-    const float2 p = ceff[off_parent + (ty >> 1) * dim_parent + (tx >> 1)];
-    ex = __fadd_rn(ex, p.x);
-    ey = __fadd_rn(ey, p.y);
-  }
-  ceff[off + ty * dim + tx] = make_float2(ex, ey);
+  m2l_tile(halo, cell4 + off, ceff + off, dim, ceff + off_parent, dim_parent, add_parent,
+           blockIdx.x * kM2LTile, blockIdx.y * kM2LTile, eps);
 }
 
 __global__ void l2l_kernel(float2* __restrict__ ceff, int off, int dim, int off_parent, int dim_parent) {

@@ -99,3 +99,65 @@ CONFIGS = {
     # a quarter of the particles on a quarter of the leaf cells: the same particles per cell as two_disks_16m
     "two_disks_4m": lambda: two_disks(1 << 22, 3, 7),
 }
+
+
+@dataclasses.dataclass
+class BatchSystem:
+    """Many independent systems: particles concatenated, per-system ranges, limits and kinds."""
+    name: str
+    position: np.ndarray   # (n, 2) float32, systems concatenated
+    weight: np.ndarray     # (n,)
+    velocity: np.ndarray   # (n, 2)
+    offsets: np.ndarray    # (S + 1,) int64
+    limits: np.ndarray     # (S, 4) float32
+    kinds: list            # "square" | "disk" per system
+    epsilon: float
+    dt: float
+    steps: int
+    grav_const: float = 1.0
+    seed: int = 0
+
+    @property
+    def n(self) -> int:
+        return int(self.offsets[-1])
+
+    @property
+    def num_systems(self) -> int:
+        return len(self.kinds)
+
+    def tick(self) -> float:
+        return float(np.float32(self.dt) * np.sqrt(np.float32(self.grav_const)))
+
+    def previous(self) -> np.ndarray:
+        t = np.float32(self.tick())
+        return (self.position - self.velocity * t).astype(np.float32)
+
+    def sizes(self) -> np.ndarray:
+        return np.diff(self.offsets)
+
+
+def batched(num_systems: int = 512, seed: int = 4, median: int = 20000, lo: int = 2000, hi: int = 262144,
+            sigma: float = 0.8) -> BatchSystem:
+    """Systems with N ~ lognormal(median 20k, log-sd 0.8: about 14M particles for 512 systems), clipped to
+    [2k, 262k]; each a uniform square (limits [-1, 1]^2) or a rotating disk (limits [-1.25, 1.25]^2) by a seeded
+    coin flip."""
+    rng = np.random.default_rng(seed)
+    sizes = np.clip(np.round(median * np.exp(rng.normal(0.0, sigma, num_systems))), lo, hi).astype(np.int64)
+    kinds = ["square" if c else "disk" for c in rng.integers(0, 2, num_systems)]
+    pos, w, vel, lim = [], [], [], []
+    for n, kind in zip(sizes, kinds):
+        if kind == "square":
+            pos.append(rng.uniform(-1.0, 1.0, (n, 2)))
+            w.append(rng.uniform(0.5, 1.5, n) / n)
+            vel.append(np.zeros((n, 2)))
+            lim.append((-1.0, -1.0, 1.0, 1.0))
+        else:
+            p, m, v = _disk(rng, int(n), 1.0, (0.0, 0.0), (0.0, 0.0))
+            pos.append(p)
+            w.append(m)
+            vel.append(v)
+            lim.append(DOMAIN)
+    offsets = np.concatenate([[0], np.cumsum(sizes)]).astype(np.int64)
+    return BatchSystem("batched", np.concatenate(pos).astype(np.float32), np.concatenate(w).astype(np.float32),
+                       np.concatenate(vel).astype(np.float32), offsets, np.asarray(lim, np.float32), kinds,
+                       1e-3, 1e-4, 100, seed=seed)
