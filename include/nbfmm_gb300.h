@@ -142,6 +142,29 @@ int nbfmm_batch_profile_begin(nbfmm_batch* batch, int max_steps);
 int nbfmm_batch_profile_end(nbfmm_batch* batch, float* p2p_ms_total, int* p2p_launches);
 int nbfmm_batch_kernel_launches(nbfmm_batch* batch, int num_steps, long long* launches);
 
+/* ---- Adjoint --------------------------------------------------------------------------------------- */
+
+/* No counterpart in the reference. Reverse mode of the engine's own approximate method through a
+ * Stormer-Verlet trajectory (solve + update.cu:39-40, no pruning inside the trajectory), for the loss
+ * L = 0.5 sum_i m_i |x_i(T) - x*_i|^2 with x_{-1} = x_0 - v_0 * tick * sqrt(grav_const). Gradients are taken
+ * with the cell assignment of every step held fixed (it is piecewise constant in the positions).
+ * Checkpoints every checkpoint_interval steps; the backward pass recomputes each segment from its checkpoint.
+ * The weight pointer given to forward must stay valid until backward returns. */
+typedef struct nbfmm_adjoint nbfmm_adjoint;
+int nbfmm_adjoint_create(int num_level, int num_particle, const float position_limits[4], float tick, float grav_const,
+                         int max_steps, int checkpoint_interval, nbfmm_adjoint** out);
+int nbfmm_adjoint_destroy(nbfmm_adjoint* adj);
+int nbfmm_adjoint_set_epsilon(nbfmm_adjoint* adj, float epsilon);
+/* Runs num_steps steps from (x0, v0) with weights m (float2/float2/float [n]); writes x(T). */
+int nbfmm_adjoint_forward(nbfmm_adjoint* adj, int num_steps, const float* gpuptr_position0,
+                          const float* gpuptr_velocity0, const float* gpuptr_weight, float* gpuptr_position_final,
+                          void* stream);
+/* dL/dx0, dL/dv0 (float2 [n]) and dL/dm (float [n]) for targets x* (float2 [n]); loss_terms (float [n], may be
+ * NULL) receives 0.5 m_i |x_i(T) - x*_i|^2. */
+int nbfmm_adjoint_backward(nbfmm_adjoint* adj, const float* gpuptr_target, float* gpuptr_grad_position0,
+                           float* gpuptr_grad_velocity0, float* gpuptr_grad_weight, float* gpuptr_loss_terms,
+                           void* stream);
+
 /* ---- Allocation-free cell sort ---------------------------------------------------------------------- */
 
 /* No counterpart in the reference. The leaf-cell sort of predo (cell keys, stable sort, heads) for callers

@@ -49,6 +49,12 @@ SIGNATURES = {
     "nbfmm_batch_profile_begin": (ctypes.c_int, [_vp, ctypes.c_int]),
     "nbfmm_batch_profile_end": (ctypes.c_int, [_vp, _c_float_p, _c_int_p]),
     "nbfmm_batch_kernel_launches": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.POINTER(ctypes.c_longlong)]),
+    "nbfmm_adjoint_create": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, _c_float_p, ctypes.c_float, ctypes.c_float,
+                                            ctypes.c_int, ctypes.c_int, ctypes.POINTER(_vp)]),
+    "nbfmm_adjoint_destroy": (ctypes.c_int, [_vp]),
+    "nbfmm_adjoint_set_epsilon": (ctypes.c_int, [_vp, ctypes.c_float]),
+    "nbfmm_adjoint_forward": (ctypes.c_int, [_vp, ctypes.c_int, _vp, _vp, _vp, _vp, _vp]),
+    "nbfmm_adjoint_backward": (ctypes.c_int, [_vp, _vp, _vp, _vp, _vp, _vp, _vp]),
     "nbfmm_sort_cells_noalloc": (ctypes.c_int, [ctypes.c_int, _c_float_p, ctypes.c_int, _vp, _vp, _vp, _vp]),
     "nbfmm_stars_profile_begin": (ctypes.c_int, [_vp, ctypes.c_int]),
     "nbfmm_stars_profile_end": (ctypes.c_int, [_vp, _c_float_p, _c_int_p]),

@@ -54,7 +54,7 @@ def build(verbose: bool = False, extra_flags=None) -> str:
         if r.returncode != 0:
             raise RuntimeError(f"nvcc failed for {cmd[-3]}")
     if _stale(LIB, objs):
-        cmd = [nvcc()] + ARCH + ["-shared", "-o", LIB] + objs
+        cmd = [nvcc()] + ARCH + ["-shared", "-Xlinker", "-z", "-Xlinker", "defs", "-o", LIB] + objs
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             sys.stderr.write(" ".join(cmd) + "\n" + r.stdout + r.stderr)

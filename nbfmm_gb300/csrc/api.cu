@@ -16,11 +16,7 @@
 #include <string>
 #include <vector>
 
-#include "../../include/nbfmm_gb300.h"
-#include "engine.cuh"
-#include "stars.cuh"
-
-using namespace nbfmm_gb300;
+#include "solver.cuh"
 
 namespace {
 
@@ -34,43 +30,6 @@ int fail(int code, const char* fmt, ...) {
   va_end(ap);
   g_last_error = buf;
   return code;
-}
-
-int cuda_check(const char* what) {
-  const cudaError_t e = cudaGetLastError();
-  if (e != cudaSuccess) return fail(NBFMM_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
-  return NBFMM_OK;
-}
-
-#define NBFMM_TRY(expr)              \
-  do {                               \
-    const int _rc = (expr);          \
-    if (_rc != NBFMM_OK) return _rc; \
-  } while (0)
-
-template <typename T>
-int dalloc(T** p, size_t count, const char* what) {
-  *p = nullptr;
-  if (count == 0) count = 1;
-  const cudaError_t e = cudaMalloc(reinterpret_cast<void**>(p), count * sizeof(T));
-  if (e != cudaSuccess) {
-    cudaGetLastError();
-    *p = nullptr;
-    return fail(e == cudaErrorMemoryAllocation ? NBFMM_ERR_NOMEM : NBFMM_ERR_CUDA, "cudaMalloc(%s, %zu bytes): %s",
-                what, count * sizeof(T), cudaGetErrorString(e));
-  }
-  return NBFMM_OK;
-}
-
-template <typename T>
-void dfree(T*& p) {
-  if (p) cudaFree(p);
-  p = nullptr;
-}
-
-bool limits_ok(const float* l) {
-  return l && std::isfinite(l[0]) && std::isfinite(l[1]) && std::isfinite(l[2]) && std::isfinite(l[3]) &&
-         l[0] < l[2] && l[1] < l[3];
 }
 
 }  // namespace
@@ -88,141 +47,6 @@ int api_fail(int code, const char* fmt, ...) {
 }
 }  // namespace nbfmm_gb300
 
-// ---- Solver --------------------------------------------------------------------------------------------
-
-struct nbfmm_solver {
-  Geometry geo{};
-  Levels lv{};
-  int max_n = 0;
-  int num_cells = 0;   // B*B
-  int key_bits = 0;    // bits of the largest key the sort sees
-  int max_tiles = 0;
-  int num_sms = 0;
-  float eps = 0.1f;
-
-  uint32_t *keys_a = nullptr, *vals_a = nullptr, *keys_b = nullptr, *vals_b = nullptr;
-  uint32_t *counts = nullptr, *digit_total = nullptr;
-  int* head = nullptr;
-  int2* work = nullptr;
-  float4* sorted4 = nullptr;
-  float2* seff = nullptr;
-  float4* cell4 = nullptr;
-  float2* ceff = nullptr;
-  int* ints = nullptr;  // [0] n, [1] n_alive, [2] work count, [3] work counter
-  // Where the last sort left its result.
-  uint32_t* skey = nullptr;
-  uint32_t* perm = nullptr;
-
-  int* d_n() { return ints + 0; }
-  int* d_n_alive() { return ints + 1; }
-  int* d_work_count() { return ints + 2; }
-  int* d_work_next() { return ints + 3; }
-
-  int init(int num_level, int max_num_particle, const float* limits, int extra_key_bits) {
-    const int B = 1 << (num_level + 1);
-    geo.xmin = limits[0];
-    geo.ymin = limits[1];
-    geo.xmax = limits[2];
-    geo.ymax = limits[3];
-    geo.cell_x = (limits[2] - limits[0]) / (float)B;  // predo.cu:112-113
-    geo.cell_y = (limits[3] - limits[1]) / (float)B;
-    geo.num_level = num_level;
-    geo.base_dim = B;
-    lv.count = num_level > 0 ? num_level : 1;
-    lv.total = 0;
-    for (int l = 0; l < lv.count; ++l) {
-      lv.dim[l] = B >> l;
-      lv.offset[l] = lv.total;
-      lv.total += lv.dim[l] * lv.dim[l];
-    }
-    max_n = max_num_particle;
-    num_cells = B * B;
-    key_bits = 2 * (num_level + 1) + extra_key_bits;
-    max_tiles = (max_n + kSortTile - 1) / kSortTile;
-    int dev = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&num_sms, cudaDevAttrMultiProcessorCount, dev);
-    NBFMM_TRY(cuda_check("device query"));
-    const size_t n = (size_t)max_n;
-    NBFMM_TRY(dalloc(&keys_a, n, "keys"));
-    NBFMM_TRY(dalloc(&vals_a, n, "values"));
-    NBFMM_TRY(dalloc(&keys_b, n, "keys"));
-    NBFMM_TRY(dalloc(&vals_b, n, "values"));
-    NBFMM_TRY(dalloc(&counts, (size_t)(1 << kRadixMaxBits) * max_tiles, "tile counts"));
-    NBFMM_TRY(dalloc(&digit_total, (size_t)(1 << kRadixMaxBits), "digit totals"));
-    NBFMM_TRY(dalloc(&head, (size_t)num_cells + 2, "head"));
-    NBFMM_TRY(dalloc(&work, (size_t)num_cells + n / kP2PChunk + 1, "work list"));
-    NBFMM_TRY(dalloc(&sorted4, n, "sorted particles"));
-    NBFMM_TRY(dalloc(&seff, n, "sorted effects"));
-    NBFMM_TRY(dalloc(&cell4, (size_t)lv.total, "cells"));
-    NBFMM_TRY(dalloc(&ceff, (size_t)lv.total, "cell effects"));
-    NBFMM_TRY(dalloc(&ints, 8, "counters"));
-    cudaMemset(ints, 0, 8 * sizeof(int));
-    cudaMemset(head, 0, ((size_t)num_cells + 2) * sizeof(int));
-    cudaMemset(cell4, 0, (size_t)lv.total * sizeof(float4));
-    cudaMemset(ceff, 0, (size_t)lv.total * sizeof(float2));
-    NBFMM_TRY(cuda_check("workspace clear"));
-    skey = keys_a;
-    perm = vals_a;
-    return NBFMM_OK;
-  }
-
-  ~nbfmm_solver() {
-    dfree(keys_a); dfree(vals_a); dfree(keys_b); dfree(vals_b);
-    dfree(counts); dfree(digit_total); dfree(head); dfree(work);
-    dfree(sorted4); dfree(seff); dfree(cell4); dfree(ceff); dfree(ints);
-  }
-
-  float4* cell0() { return cell4 + lv.offset[0]; }
-  float2* ceff0() { return ceff + lv.offset[0]; }
-
-  // Sort (keys_a, vals_a) holding d_n entries; records where the result went.
-  void sort(const int* dn, int bits, cudaStream_t s) {
-    const int where = launch_radix_sort(keys_a, vals_a, keys_b, vals_b, counts, digit_total, dn, max_n, bits, s);
-    skey = where ? keys_b : keys_a;
-    perm = where ? vals_b : vals_a;
-  }
-
-  // Keys, sort, head and work list from caller-order positions (predo.cu:105-135 minus the gather).
-  void preassign(int n, const float2* pos, cudaStream_t s) {
-    launch_set_int(d_n(), n, s);
-    launch_keys_from_positions(geo, pos, d_n(), keys_a, vals_a, max_n, s);
-    sort(d_n(), key_bits, s);
-    launch_head(skey, d_n(), num_cells, head, d_n_alive(), s);
-    launch_worklist(head, num_cells, work, d_work_count(), s);
-  }
-
-  void far_field(cudaStream_t s) {
-    if (geo.num_level <= 0) return;  // p2m.cu:80, m2l.cu:64
-    launch_m2m(lv, cell4, s);         // no-op for num_level <= 1 (m2m.cu:60)
-    launch_m2l(lv, cell4, ceff, eps, true, s);
-  }
-
-  P2PArgs p2p_args() {
-    P2PArgs a{};
-    a.sorted4 = sorted4;
-    a.head = head;
-    a.work = work;
-    a.d_work_count = d_work_count();
-    a.d_work_next = d_work_next();
-    a.base_dim = geo.base_dim;
-    a.eps = eps;
-    a.ceff0 = geo.num_level > 0 ? ceff0() : nullptr;
-    return a;
-  }
-
-  int solve(int n, const float* pos, const float* w, float* eff, cudaStream_t s) {
-    if (n == 0) return NBFMM_OK;
-    preassign(n, reinterpret_cast<const float2*>(pos), s);
-    launch_gather_p2m(geo, head, perm, reinterpret_cast<const float2*>(pos), w, sorted4, cell0(), s);
-    far_field(s);
-    P2PArgs a = p2p_args();
-    a.eff_origin = reinterpret_cast<float2*>(eff);
-    launch_p2p(a, kSolve, num_sms, s);
-    return cuda_check("nbfmm_solver_solve");
-  }
-};
-
 namespace {
 
 int check_solver(nbfmm_solver* h) { return h ? NBFMM_OK : fail(NBFMM_ERR_INVALID, "null solver handle"); }
@@ -234,7 +58,9 @@ int check_n(nbfmm_solver* h, int n) {
   return NBFMM_OK;
 }
 
-int make_solver(int num_level, int max_num_particle, const float* limits, int extra_key_bits, nbfmm_solver** out) {
+}  // namespace
+
+int nbfmm_make_solver(int num_level, int max_num_particle, const float* limits, int extra_key_bits, nbfmm_solver** out) {
   if (!out) return fail(NBFMM_ERR_INVALID, "null output pointer");
   *out = nullptr;
   if (num_level < 0 || num_level > kMaxLevels - 1) {
@@ -255,6 +81,8 @@ int make_solver(int num_level, int max_num_particle, const float* limits, int ex
   return NBFMM_OK;
 }
 
+namespace {
+
 cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s); }
 
 }  // namespace
@@ -266,7 +94,7 @@ const char* nbfmm_last_error(void) { return g_last_error.c_str(); }
 int nbfmm_version(void) { return NBFMM_GB300_VERSION; }
 
 int nbfmm_solver_create(int num_level, int max_num_particle, const float position_limits[4], nbfmm_solver** out) {
-  return make_solver(num_level, max_num_particle, position_limits, 0, out);
+  return nbfmm_make_solver(num_level, max_num_particle, position_limits, 0, out);
 }
 
 int nbfmm_solver_destroy(nbfmm_solver* solver) {
@@ -423,7 +251,7 @@ struct nbfmm_stars {
   int prof_max = 0, prof_used = 0;
 
   int init(int fmm_level, int num_star, float tick_scaled, const float* limits) {
-    NBFMM_TRY(make_solver(fmm_level, num_star > 0 ? num_star : 1, limits, 1, &solver));
+    NBFMM_TRY(nbfmm_make_solver(fmm_level, num_star > 0 ? num_star : 1, limits, 1, &solver));
     max_n = num_star > 0 ? num_star : 1;
     tick = tick_scaled;
     const size_t n = (size_t)max_n;

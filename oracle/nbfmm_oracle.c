@@ -483,3 +483,252 @@ long long orc_p2p_pairs(int base_dim, const int* head) {
   }
   return total;
 }
+
+/* ---- FP64 checkers for the adjoint ------------------------------------------------------------------------ */
+
+/* Effects of the approximate method in FP64 for positions x (double [2n]) with the leaf key of every particle
+ * given: the same stages as orc_solve (p2p.cu, p2m.cu, m2m.cu, m2l.cu, l2l.cu, l2p.cu) in double precision. */
+static void fmm64_effects(int n, int num_level, const int* key, const double* x, const double* m, double eps,
+                          double* a) {
+  const int B = orc_base_dim(num_level);
+  const int C = B * B;
+  const int levels = num_level < 2 ? 2 : num_level;
+  int* cnt = (int*)calloc((size_t)C + 1, sizeof(int));
+  int* head = (int*)malloc(sizeof(int) * ((size_t)C + 1));
+  int* perm = (int*)malloc(sizeof(int) * (size_t)n);
+  double* cp = (double*)calloc(2 * (size_t)C * levels, sizeof(double));
+  double* cw = (double*)calloc((size_t)C * levels, sizeof(double));
+  double* ce = (double*)calloc(2 * (size_t)C * levels, sizeof(double));
+  for (int i = 0; i < n; ++i) cnt[key[i]]++;
+  int run = 0;
+  for (int c = 0; c < C; ++c) { head[c] = run; run += cnt[c]; }
+  head[C] = run;
+  for (int c = 0; c < C; ++c) cnt[c] = head[c];
+  for (int i = 0; i < n; ++i) perm[cnt[key[i]]++] = i;
+  for (int i = 0; i < n; ++i) {
+    const int cx = key[i] % B, cy = key[i] / B;
+    double ex = 0.0, ey = 0.0;
+    for (int y = cy - 1; y <= cy + 1; ++y) {
+      for (int xx = cx - 1; xx <= cx + 1; ++xx) {
+        if (xx < 0 || xx >= B || y < 0 || y >= B) continue;
+        const int c = xx + y * B;
+        for (int q = head[c]; q < head[c + 1]; ++q) {
+          const int j = perm[q];
+          if (j == i) continue;
+          const double dx = x[2 * j] - x[2 * i], dy = x[2 * j + 1] - x[2 * i + 1];
+          const double r = sqrt(dx * dx + dy * dy);
+          const double s = m[j] / (r * r * r + eps);
+          ex += dx * s;
+          ey += dy * s;
+        }
+      }
+    }
+    a[2 * i] = ex;
+    a[2 * i + 1] = ey;
+  }
+  if (num_level > 0) {
+    for (int c = 0; c < C; ++c) {
+      double sx = 0.0, sy = 0.0, sw = 0.0;
+      for (int q = head[c]; q < head[c + 1]; ++q) {
+        const int j = perm[q];
+        sx += x[2 * j] * m[j];
+        sy += x[2 * j + 1] * m[j];
+        sw += m[j];
+      }
+      cp[2 * c] = sw != 0.0 ? sx / sw : 0.0;
+      cp[2 * c + 1] = sw != 0.0 ? sy / sw : 0.0;
+      cw[c] = sw;
+    }
+    for (int level = 1; level < num_level; ++level) {
+      const int cs = 1 << level, ld = B / cs;
+      double* lp = cp + 2 * (size_t)level * C;
+      double* lw = cw + (size_t)level * C;
+      for (int ty = 0; ty < ld; ++ty) {
+        for (int tx = 0; tx < ld; ++tx) {
+          const int idx = (tx + ty * B) * cs, ch = idx - C, ox = cs / 2, oy = ox * B;
+          const int cc[4] = {ch, ch + ox, ch + oy, ch + ox + oy};
+          double px = 0.0, py = 0.0, ww = 0.0;
+          for (int k = 0; k < 4; ++k) {
+            px += lp[2 * cc[k]] * lw[cc[k]];
+            py += lp[2 * cc[k] + 1] * lw[cc[k]];
+            ww += lw[cc[k]];
+          }
+          lp[2 * idx] = ww != 0.0 ? px / ww : 0.0;
+          lp[2 * idx + 1] = ww != 0.0 ? py / ww : 0.0;
+          lw[idx] = ww;
+        }
+      }
+    }
+    for (int level = 0; level < num_level; ++level) {
+      const int cs = 1 << level, ld = B >> level;
+      const double* lp = cp + 2 * (size_t)level * C;
+      const double* lw = cw + (size_t)level * C;
+      double* le = ce + 2 * (size_t)level * C;
+      for (int ty = 0; ty < ld; ++ty) {
+        for (int tx = 0; tx < ld; ++tx) {
+          const int px = tx & ~1, py = ty & ~1, tidx = (tx + ty * B) * cs;
+          double ex = 0.0, ey = 0.0;
+          for (int y = py - 2; y < py + 4; ++y) {
+            if (y < 0 || y >= ld) continue;
+            for (int xx = px - 2; xx < px + 4; ++xx) {
+              if (xx < 0 || xx >= ld) continue;
+              if (abs(xx - tx) > 1 || abs(y - ty) > 1) {
+                const int idx = (xx + y * B) * cs;
+                const double dx = lp[2 * idx] - lp[2 * tidx], dy = lp[2 * idx + 1] - lp[2 * tidx + 1];
+                const double r = sqrt(dx * dx + dy * dy);
+                const double s = lw[idx] / (r * r * r + eps);
+                ex += dx * s;
+                ey += dy * s;
+              }
+            }
+          }
+          le[2 * tidx] = ex;
+          le[2 * tidx + 1] = ey;
+        }
+      }
+    }
+    for (int level = num_level - 2; level >= 0; --level) {
+      const int cs = 1 << level, ld = B / cs;
+      double* le = ce + 2 * (size_t)level * C;
+      for (int ty = 0; ty < ld; ++ty) {
+        for (int tx = 0; tx < ld; ++tx) {
+          const int idx = (tx + ty * B) * cs, par = ((tx & ~1) + (ty & ~1) * B) * cs + C;
+          le[2 * idx] += le[2 * par];
+          le[2 * idx + 1] += le[2 * par + 1];
+        }
+      }
+    }
+    for (int i = 0; i < n; ++i) {
+      a[2 * i] += ce[2 * key[i]];
+      a[2 * i + 1] += ce[2 * key[i] + 1];
+    }
+  }
+  free(cnt); free(head); free(perm); free(cp); free(cw); free(ce);
+}
+
+/* FP64 trajectory of the approximate method (update.cu:39-40 without pruning) from x_{-1} = x0 - v0 tau.
+ * keys_in (steps x n) fixes the leaf of every particle at every step; when NULL the keys come from the FP32
+ * cell arithmetic on the current positions and are written to keys_out (may be NULL). Returns the loss
+ * 0.5 sum m |x(T) - target|^2 and writes x(T) to xT (may be NULL). */
+double orc_traj_fmm64(int n, int num_level, const float limits[4], double eps, double tau, int steps,
+                      const double* x0, const double* v0, const double* m, const int* keys_in, int* keys_out,
+                      const double* target, double* xT) {
+  const int B = orc_base_dim(num_level);
+  double* x = (double*)malloc(sizeof(double) * 2 * (size_t)n);
+  double* xp = (double*)malloc(sizeof(double) * 2 * (size_t)n);
+  double* a = (double*)malloc(sizeof(double) * 2 * (size_t)n);
+  int* key = (int*)malloc(sizeof(int) * (size_t)n);
+  for (int i = 0; i < 2 * n; ++i) {
+    x[i] = x0[i];
+    xp[i] = x0[i] - v0[i] * tau;
+  }
+  for (int t = 0; t < steps; ++t) {
+    const int* k = keys_in ? keys_in + (size_t)t * n : key;
+    if (!keys_in) {
+      for (int i = 0; i < n; ++i) {
+        int ix, iy;
+        orc_cell_index(limits, B, (float)x[2 * i], (float)x[2 * i + 1], &ix, &iy);
+        key[i] = ix + iy * B;
+      }
+      if (keys_out) memcpy(keys_out + (size_t)t * n, key, sizeof(int) * (size_t)n);
+    }
+    fmm64_effects(n, num_level, k, x, m, eps, a);
+    for (int i = 0; i < 2 * n; ++i) {
+      const double p = x[i];
+      x[i] = 2.0 * p - xp[i] + a[i] * tau * tau;
+      xp[i] = p;
+    }
+  }
+  double loss = 0.0;
+  for (int i = 0; i < n; ++i) {
+    const double dx = x[2 * i] - target[2 * i], dy = x[2 * i + 1] - target[2 * i + 1];
+    loss += 0.5 * m[i] * (dx * dx + dy * dy);
+  }
+  if (xT) memcpy(xT, x, sizeof(double) * 2 * (size_t)n);
+  free(x); free(xp); free(a); free(key);
+  return loss;
+}
+
+/* The exact all-pairs dynamics in FP64 and the exact gradient of its loss by the adjoint (reverse Verlet with
+ * the all-pairs vector-Jacobian products). Returns the loss. */
+double orc_traj_direct64_grad(int n, double eps, double tau, int steps, const double* x0, const double* v0,
+                              const double* m, const double* target, double* gx0, double* gv0, double* gm) {
+  double* xs = (double*)malloc(sizeof(double) * 2 * (size_t)n * (steps + 1));
+  double* xp = (double*)malloc(sizeof(double) * 2 * (size_t)n);
+  double* a = (double*)malloc(sizeof(double) * 2 * (size_t)n);
+  for (int i = 0; i < 2 * n; ++i) {
+    xs[i] = x0[i];
+    xp[i] = x0[i] - v0[i] * tau;
+  }
+  for (int t = 0; t < steps; ++t) {
+    const double* x = xs + (size_t)t * 2 * n;
+    double* xn = xs + (size_t)(t + 1) * 2 * n;
+#pragma omp parallel for schedule(static)
+    for (int i = 0; i < n; ++i) {
+      double ex = 0.0, ey = 0.0;
+      for (int j = 0; j < n; ++j) {
+        if (j == i) continue;
+        const double dx = x[2 * j] - x[2 * i], dy = x[2 * j + 1] - x[2 * i + 1];
+        const double r = sqrt(dx * dx + dy * dy);
+        const double s = m[j] / (r * r * r + eps);
+        ex += dx * s;
+        ey += dy * s;
+      }
+      a[2 * i] = ex;
+      a[2 * i + 1] = ey;
+    }
+    for (int i = 0; i < 2 * n; ++i) {
+      xn[i] = 2.0 * x[i] - xp[i] + a[i] * tau * tau;
+      xp[i] = x[i];
+    }
+  }
+  const double* xT = xs + (size_t)steps * 2 * n;
+  double loss = 0.0;
+  double* l1 = (double*)malloc(sizeof(double) * 2 * (size_t)n);  /* lambda_{t+1} */
+  double* l2 = (double*)calloc(2 * (size_t)n, sizeof(double));   /* lambda_{t+2} */
+  double* g = (double*)malloc(sizeof(double) * 2 * (size_t)n);
+  double* gmv = (double*)malloc(sizeof(double) * (size_t)n);
+  for (int i = 0; i < n; ++i) {
+    const double dx = xT[2 * i] - target[2 * i], dy = xT[2 * i + 1] - target[2 * i + 1];
+    loss += 0.5 * m[i] * (dx * dx + dy * dy);
+    l1[2 * i] = m[i] * dx;
+    l1[2 * i + 1] = m[i] * dy;
+    gm[i] = 0.5 * (dx * dx + dy * dy);
+  }
+  for (int t = steps - 1; t >= 0; --t) {
+    const double* x = xs + (size_t)t * 2 * n;
+#pragma omp parallel for schedule(static)
+    for (int i = 0; i < n; ++i) {
+      const double mux = tau * tau * l1[2 * i], muy = tau * tau * l1[2 * i + 1];
+      double gx = 0.0, gy = 0.0, gmi = 0.0;
+      for (int j = 0; j < n; ++j) {
+        if (j == i) continue;
+        const double dx = x[2 * j] - x[2 * i], dy = x[2 * j + 1] - x[2 * i + 1];
+        const double r = sqrt(dx * dx + dy * dy);
+        const double inv = 1.0 / (r * r * r + eps);
+        const double mjx = tau * tau * l1[2 * j], mjy = tau * tau * l1[2 * j + 1];
+        const double ux = m[i] * mjx - m[j] * mux, uy = m[i] * mjy - m[j] * muy;
+        const double k3 = 3.0 * r * inv * inv * (dx * ux + dy * uy);
+        gx += ux * inv - k3 * dx;
+        gy += uy * inv - k3 * dy;
+        gmi -= (mjx * dx + mjy * dy) * inv;
+      }
+      g[2 * i] = gx;
+      g[2 * i + 1] = gy;
+      gmv[i] = gmi;
+    }
+    for (int i = 0; i < 2 * n; ++i) {
+      const double l0 = 2.0 * l1[i] + g[i] - l2[i];
+      l2[i] = l1[i];
+      l1[i] = l0;
+    }
+    for (int i = 0; i < n; ++i) gm[i] += gmv[i];
+  }
+  /* now l1 = lambda_0, l2 = lambda_1 */
+  for (int i = 0; i < 2 * n; ++i) {
+    gx0[i] = l1[i] - l2[i];
+    gv0[i] = tau * l2[i];
+  }
+  free(xs); free(xp); free(a); free(l1); free(l2); free(g); free(gmv);
+  return loss;
+}

@@ -93,6 +93,17 @@ void orc_direct_f64(int n, const float* pos, const float* w, double eps, const i
 /* Number of P2P pairs of a sorted system (targets x sources over each 3x3 block, self excluded). */
 long long orc_p2p_pairs(int base_dim, const int* head);
 
+/* FP64 trajectory of the approximate method from x_{-1} = x0 - v0 tau, no pruning, with the leaf of every
+ * particle at every step given by keys_in (steps x n) or, when keys_in is NULL, computed from the positions
+ * with the FP32 cell arithmetic and written to keys_out (may be NULL). Returns 0.5 sum m |x(T) - target|^2. */
+double orc_traj_fmm64(int n, int num_level, const float limits[4], double eps, double tau, int steps,
+                      const double* x0, const double* v0, const double* m, const int* keys_in, int* keys_out,
+                      const double* target, double* xT);
+
+/* Exact all-pairs FP64 dynamics and the exact gradient of the same loss by its adjoint. Returns the loss. */
+double orc_traj_direct64_grad(int n, double eps, double tau, int steps, const double* x0, const double* v0,
+                              const double* m, const double* target, double* gx0, double* gv0, double* gm);
+
 /* Number of OpenMP threads the oracle will use. */
 int orc_num_threads(void);
 

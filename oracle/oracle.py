@@ -50,6 +50,10 @@ def lib():
             "orc_direct_f64": (None, [c_int, _f, _f, ctypes.c_double, ctypes.c_void_p, c_int, _d]),
             "orc_p2p_pairs": (ctypes.c_longlong, [c_int, _i]),
             "orc_num_threads": (c_int, []),
+            "orc_traj_fmm64": (ctypes.c_double, [c_int, c_int, _f, ctypes.c_double, ctypes.c_double, c_int, _d, _d, _d,
+                                                 ctypes.c_void_p, ctypes.c_void_p, _d, ctypes.c_void_p]),
+            "orc_traj_direct64_grad": (ctypes.c_double, [c_int, ctypes.c_double, ctypes.c_double, c_int, _d, _d, _d, _d,
+                                                         _d, _d, _d]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(L, name)
@@ -198,3 +202,27 @@ def ref_lib():
     L.ref_weighted_position.argtypes = [ctypes.c_int, _f, _f, _f]
     L.ref_weighted_position.restype = None
     return L
+
+
+def f64(a):
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+def traj_fmm64(x0, v0, m, num_level, limits, eps, tau, steps, target, keys=None):
+    """FP64 loss of the approximate method's trajectory; returns (loss, keys used (steps, n))."""
+    n = len(m)
+    keys_out = np.zeros((steps, n), np.int32) if keys is None else None
+    kin = None if keys is None else i32(keys).ctypes.data_as(ctypes.c_void_p)
+    kout = None if keys_out is None else keys_out.ctypes.data_as(ctypes.c_void_p)
+    loss = lib().orc_traj_fmm64(n, num_level, lim(limits), float(eps), float(tau), steps, f64(x0).reshape(-1),
+                                f64(v0).reshape(-1), f64(m), kin, kout, f64(target).reshape(-1), None)
+    return loss, (keys if keys is not None else keys_out)
+
+
+def traj_direct64_grad(x0, v0, m, eps, tau, steps, target):
+    """(loss, dL/dx0, dL/dv0, dL/dm) of the exact all-pairs FP64 dynamics."""
+    n = len(m)
+    gx, gv, gm = np.zeros(2 * n), np.zeros(2 * n), np.zeros(n)
+    loss = lib().orc_traj_direct64_grad(n, float(eps), float(tau), steps, f64(x0).reshape(-1), f64(v0).reshape(-1),
+                                        f64(m), f64(target).reshape(-1), gx, gv, gm)
+    return loss, gx.reshape(n, 2), gv.reshape(n, 2), gm
