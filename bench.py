@@ -266,12 +266,76 @@ def run_batched(args):
     print(json.dumps(out), flush=True)
 
 
+def run_adjoint(args):
+    """Adjoint through the trajectory: forward pass and backward pass of the 262,144-particle disk (depth 6),
+    dt 1e-4, checkpoints every 20 steps; targets = forward final positions + N(0, 1e-3)."""
+    import torch
+
+    import nbfmm_gb300
+    from nbfmm_gb300 import workloads
+    from nbfmm_gb300.adjoint import Adjoint
+
+    sysm = workloads.disk(1 << 18, seed=5, num_level=5)
+    steps = args.steps
+    n = sysm.n
+    f = lambda a: torch.from_numpy(np.ascontiguousarray(a, np.float32)).cuda()
+    x0, v0, m = f(sysm.position), f(sysm.velocity), f(sysm.weight)
+    adj = Adjoint(sysm.num_level, n, sysm.limits, tick=sysm.dt, max_steps=steps, checkpoint_interval=20,
+                  epsilon=sysm.epsilon)
+    xT = torch.empty_like(x0)
+    adj.forward(steps, x0, v0, m, xT)
+    torch.cuda.synchronize()
+    g = torch.Generator(device="cpu").manual_seed(5)
+    target = (xT.cpu() + 1e-3 * torch.randn(xT.shape, generator=g)).cuda()
+    gx, gv, gm, terms = torch.empty_like(x0), torch.empty_like(v0), torch.empty_like(m), torch.empty_like(m)
+    for _ in range(max(1, args.warmup)):
+        adj.forward(steps, x0, v0, m, xT)
+        adj.backward(target, gx, gv, gm, terms)
+    torch.cuda.synchronize()
+    e = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+    clocks = ClockSampler("0")
+    e[0].record()
+    adj.forward(steps, x0, v0, m, xT)
+    e[1].record()
+    adj.backward(target, gx, gv, gm, terms)
+    e[2].record()
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    fwd = e[0].elapsed_time(e[1])
+    bwd = e[1].elapsed_time(e[2])
+    # the graph-replayed Stars step of the same system, for reference
+    st = nbfmm_gb300.Stars(sysm.num_level, n, tick=sysm.dt, position_limits=sysm.limits, epsilon=sysm.epsilon)
+    st.gpuptr_position_cur_.copy_(x0)
+    st.gpuptr_position_pre_.copy_(f(sysm.previous()))
+    st.gpuptr_weight_.copy_(m)
+    st.update(3)
+    torch.cuda.synchronize()
+    e[0].record()
+    st.update(steps)
+    e[1].record()
+    torch.cuda.synchronize()
+    stars_ms = e[0].elapsed_time(e[1])
+    out = {
+        "metric": "adjoint/forward time", "value": bwd / fwd, "unit": "ratio", "higher_is_better": False,
+        "n_gpus": 1, "steps": steps, "warmup": args.warmup, "dtype": "f32", "data": "synthetic (seeded disk)",
+        "config": {"workload": f"adjoint: disk N={n:,}, depth 6, dt {sysm.dt:g}, eps {sysm.epsilon:g}, "
+                               f"{steps} steps, checkpoint every 20, loss 0.5 sum m |x(T) - x*|^2"},
+        "forward_ms_per_step": fwd / steps, "backward_ms_per_step": bwd / steps,
+        "adjoint_total_over_forward": (fwd + bwd) / fwd,
+        "stars_update_ms_per_step": stars_ms / steps, "backward_over_stars_step": bwd / stars_ms,
+        "particle_steps_per_s_forward": n * steps / (fwd / 1e3), "clocks": clk,
+    }
+    print(json.dumps(out), flush=True)
+
+
 def main():
     args = parse()
     from nbfmm_gb300 import workloads
 
     if args.config == "batched_512" and args.impl == "gb300":
         return run_batched(args)
+    if args.config == "adjoint_262k" and args.impl == "gb300":
+        return run_adjoint(args)
 
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))

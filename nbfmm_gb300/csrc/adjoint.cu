@@ -160,20 +160,206 @@ struct AdjP2PArgs {
   float* gm_out;          // original order
 };
 
+typedef unsigned long long f2x;  // two packed floats
+
+__device__ __forceinline__ f2x pk(float lo, float hi) {
+  f2x r;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
+  return r;
+}
+
+__device__ __forceinline__ void up(f2x v, float& lo, float& hi) {
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v));
+}
+
+__device__ __forceinline__ f2x sub2(f2x a, f2x b) {
+  f2x r;
+  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+  return r;
+}
+
+__device__ __forceinline__ f2x mul2(f2x a, f2x b) {
+  f2x r;
+  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+  return r;
+}
+
+__device__ __forceinline__ f2x fma2(f2x a, f2x b, f2x c) {
+  f2x r;
+  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c));
+  return r;
+}
+
+// A warp's 32-source batch, packed for f32x2: (x, x, y, y), (mu_x, mu_x, mu_y, mu_y), (-m, -m).
 struct AdjSlice {
-  float4 p[32];   // x, y, m, -
-  float2 mu[32];
+  ulonglong2 xy[32];
+  ulonglong2 mu[32];
+  f2x mneg[32];
 };
 
-// Reverse near field + the transposed P2M of the far field, one warp per work item, sources in 32-wide slices.
-__global__ void __launch_bounds__(kAdjWarps * 32)
-adj_p2p_kernel(const AdjP2PArgs a) {
+// Per pair (d = x_j - x_i, D = r^3 + eps): u = m_i mu_j - m_j mu_i, g_x += u/D - 3 r (d.u) d / D^2,
+// s_m += (mu_j . d) / D (g_m = -s_m). Both targets of a packed pair share the source.
+struct AdjTargets2 {
+  f2x x, y, m, mux, muy;
+  f2x gx, gy, sm;
+};
+
+__device__ __forceinline__ void adj_pair2(AdjTargets2& t, f2x sx, f2x sy, f2x mjx, f2x mjy, f2x mjneg, f2x eps2,
+                                          f2x neg3) {
+  const f2x dx = sub2(sx, t.x);
+  const f2x dy = sub2(sy, t.y);
+  const f2x r2 = fma2(dy, dy, mul2(dx, dx));
+  float r2a, r2b;
+  up(r2, r2a, r2b);
+  const f2x r = pk(sqrt_approx(r2a), sqrt_approx(r2b));
+  float da, db;
+  up(fma2(r2, r, eps2), da, db);
+  const f2x inv = pk(rcp_approx(da), rcp_approx(db));
+  const f2x ux = fma2(t.m, mjx, mul2(mjneg, t.mux));
+  const f2x uy = fma2(t.m, mjy, mul2(mjneg, t.muy));
+  const f2x du = fma2(dy, uy, mul2(dx, ux));
+  const f2x w = mul2(mul2(mul2(r, neg3), mul2(inv, inv)), du);
+  t.gx = fma2(w, dx, fma2(ux, inv, t.gx));
+  t.gy = fma2(w, dy, fma2(uy, inv, t.gy));
+  t.sm = fma2(fma2(dy, mjy, mul2(dx, mjx)), inv, t.sm);
+}
+
+struct AdjTarget1 {
+  float x, y, m, mux, muy;
+  float gx, gy, sm;
+};
+
+__device__ __forceinline__ void adj_pair1(AdjTarget1& t, float sx, float sy, float mjx, float mjy, float mjneg,
+                                          float eps) {
+  const float dx = sx - t.x, dy = sy - t.y;
+  const float r2 = fmaf(dy, dy, dx * dx);
+  const float r = sqrt_approx(r2);
+  const float inv = rcp_approx(fmaf(r2, r, eps));
+  const float ux = fmaf(t.m, mjx, mjneg * t.mux);
+  const float uy = fmaf(t.m, mjy, mjneg * t.muy);
+  const float w = -3.0f * r * inv * inv * fmaf(dy, uy, dx * ux);
+  t.gx = fmaf(w, dx, fmaf(ux, inv, t.gx));
+  t.gy = fmaf(w, dy, fmaf(uy, inv, t.gy));
+  t.sm = fmaf(fmaf(dy, mjy, dx * mjx), inv, t.sm);
+}
+
+struct AdjRanges {
+  int s0, l0, s1, l1, s2, l2;
+  __device__ __forceinline__ int total() const { return l0 + l1 + l2; }
+  __device__ __forceinline__ int at(int s) const {
+    return (s < l0) ? s0 + s : (s < l0 + l1) ? s1 + (s - l0) : s2 + (s - l0 - l1);
+  }
+};
+
+__device__ __forceinline__ void adj_epilogue(const AdjP2PArgs& a, int j, int cell, float x, float y, float m,
+                                             float gx, float gy, float sm) {
+  float rm = -sm;
+  if (a.cell0) {  // transposed P2M of the far field
+    const float4 c = a.cell0[cell];
+    const float4 g = a.g0[cell];
+    if (c.z != 0.0f) {
+      gx += (m / c.z) * g.x;
+      gy += (m / c.z) * g.y;
+      rm += g.z + (g.x * (x - c.x) + g.y * (y - c.y)) / c.z;
+    }
+  }
+  const int orig = __float_as_int(a.sorted4[j].w);
+  a.gx_out[orig] = make_float2(gx, gy);
+  a.gm_out[orig] = rm;
+}
+
+template <int NP, int ODD>
+__device__ __forceinline__ void adj_item(const AdjP2PArgs& a, AdjSlice& sl, int lane, int cell, int first, int last,
+                                         const AdjRanges& rg) {
+  constexpr int kPasses = 2 * NP + ODD;
+  float tx[kPasses], ty[kPasses], tm[kPasses], tux[kPasses], tuy[kPasses];
+#pragma unroll
+  for (int p = 0; p < kPasses; ++p) {
+    const int j = first + p * 32 + lane;
+    const bool v = j < last;
+    const float4 q = v ? a.sorted4[j] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    const float2 u = v ? a.smu[j] : make_float2(0.0f, 0.0f);
+    tx[p] = q.x; ty[p] = q.y; tm[p] = q.z; tux[p] = u.x; tuy[p] = u.y;
+  }
+  AdjTargets2 T[NP > 0 ? NP : 1];
+#pragma unroll
+  for (int q = 0; q < NP; ++q) {
+    T[q].x = pk(tx[2 * q], tx[2 * q + 1]);
+    T[q].y = pk(ty[2 * q], ty[2 * q + 1]);
+    T[q].m = pk(tm[2 * q], tm[2 * q + 1]);
+    T[q].mux = pk(tux[2 * q], tux[2 * q + 1]);
+    T[q].muy = pk(tuy[2 * q], tuy[2 * q + 1]);
+    T[q].gx = 0ull;
+    T[q].gy = 0ull;
+    T[q].sm = 0ull;
+  }
+  AdjTarget1 O{tx[kPasses - 1], ty[kPasses - 1], tm[kPasses - 1], tux[kPasses - 1], tuy[kPasses - 1], 0.0f, 0.0f, 0.0f};
+  const float eps = a.eps;
+  const f2x eps2 = pk(eps, eps);
+  const f2x neg3 = pk(-3.0f, -3.0f);
+  const int total = rg.total();
+  float4 nq = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+  float2 nu = make_float2(0.0f, 0.0f);
+  if (lane < total) {
+    const int g = rg.at(lane);
+    nq = a.sorted4[g];
+    nu = a.smu[g];
+  }
+  for (int base = 0; base < total; base += 32) {
+    __syncwarp();
+    sl.xy[lane] = make_ulonglong2(pk(nq.x, nq.x), pk(nq.y, nq.y));
+    sl.mu[lane] = make_ulonglong2(pk(nu.x, nu.x), pk(nu.y, nu.y));
+    sl.mneg[lane] = pk(-nq.z, -nq.z);  // beyond `total` the source is massless with mu = 0: an exact zero
+    __syncwarp();
+    nq = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    nu = make_float2(0.0f, 0.0f);
+    if (base + 32 + lane < total) {
+      const int g = rg.at(base + 32 + lane);
+      nq = a.sorted4[g];
+      nu = a.smu[g];
+    }
+#pragma unroll 4
+    for (int k = 0; k < 32; ++k) {
+      const ulonglong2 s = sl.xy[k];
+      const ulonglong2 u = sl.mu[k];
+      const f2x mn = sl.mneg[k];
+#pragma unroll
+      for (int q = 0; q < NP; ++q) adj_pair2(T[q], s.x, s.y, u.x, u.y, mn, eps2, neg3);
+      if (ODD) {
+        float sx, sy, ux, uy, m, dummy;
+        up(s.x, sx, dummy);
+        up(s.y, sy, dummy);
+        up(u.x, ux, dummy);
+        up(u.y, uy, dummy);
+        up(mn, m, dummy);
+        adj_pair1(O, sx, sy, ux, uy, m, eps);
+      }
+    }
+  }
+#pragma unroll
+  for (int q = 0; q < NP; ++q) {
+    float gx0, gx1, gy0, gy1, s0, s1;
+    up(T[q].gx, gx0, gx1);
+    up(T[q].gy, gy0, gy1);
+    up(T[q].sm, s0, s1);
+    const int j0 = first + (2 * q) * 32 + lane, j1 = j0 + 32;
+    if (j0 < last) adj_epilogue(a, j0, cell, tx[2 * q], ty[2 * q], tm[2 * q], gx0, gy0, s0);
+    if (j1 < last) adj_epilogue(a, j1, cell, tx[2 * q + 1], ty[2 * q + 1], tm[2 * q + 1], gx1, gy1, s1);
+  }
+  if (ODD) {
+    const int j = first + (kPasses - 1) * 32 + lane;
+    if (j < last) adj_epilogue(a, j, cell, O.x, O.y, O.m, O.gx, O.gy, O.sm);
+  }
+}
+
+// Reverse near field + the transposed P2M of the far field. Warps are independent and take (cell, up to 128
+// targets) items; the item's sources stream through the warp's own 32-source slice.
+__global__ void __launch_bounds__(kAdjWarps * 32, 4) adj_p2p_kernel(const AdjP2PArgs a) {
   __shared__ AdjSlice slices[kAdjWarps];
   const int lane = threadIdx.x & 31;
   AdjSlice& sl = slices[threadIdx.x >> 5];
   const int B = a.base_dim;
   const int work_count = *a.d_work_count;
-  const float eps = a.eps;
   for (;;) {
     int item = 0;
     if (lane == 0) item = atomicAdd(a.d_work_next, 1);
@@ -184,82 +370,18 @@ adj_p2p_kernel(const AdjP2PArgs a) {
     const int cx = cell % B, cy = cell / B;
     const int lo = cx > 0 ? cx - 1 : 0;
     const int hi = cx + 1 < B ? cx + 1 : B - 1;
-    int s0 = 0, l0 = 0, s1, l1, s2 = 0, l2 = 0;
-    if (cy > 0) { s0 = a.head[lo + (cy - 1) * B]; l0 = a.head[hi + (cy - 1) * B + 1] - s0; }
-    s1 = a.head[lo + cy * B];
-    l1 = a.head[hi + cy * B + 1] - s1;
-    if (cy + 1 < B) { s2 = a.head[lo + (cy + 1) * B]; l2 = a.head[hi + (cy + 1) * B + 1] - s2; }
-    const int total = l0 + l1 + l2;
+    AdjRanges rg{0, 0, 0, 0, 0, 0};
+    if (cy > 0) { rg.s0 = a.head[lo + (cy - 1) * B]; rg.l0 = a.head[hi + (cy - 1) * B + 1] - rg.s0; }
+    rg.s1 = a.head[lo + cy * B];
+    rg.l1 = a.head[hi + cy * B + 1] - rg.s1;
+    if (cy + 1 < B) { rg.s2 = a.head[lo + (cy + 1) * B]; rg.l2 = a.head[hi + (cy + 1) * B + 1] - rg.s2; }
     const int first = a.head[cell] + wc.y * kP2PChunk;
     const int last = min(first + kP2PChunk, a.head[cell + 1]);
-    // up to 4 targets per lane
-    float tx[kP2PPasses], ty[kP2PPasses], tm[kP2PPasses], ux[kP2PPasses], uy[kP2PPasses];
-    float gx[kP2PPasses], gy[kP2PPasses], gm[kP2PPasses];
-#pragma unroll
-    for (int p = 0; p < kP2PPasses; ++p) {
-      const int j = first + p * 32 + lane;
-      const bool v = j < last;
-      const float4 q = v ? a.sorted4[j] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-      const float2 m = v ? a.smu[j] : make_float2(0.0f, 0.0f);
-      tx[p] = q.x; ty[p] = q.y; tm[p] = q.z; ux[p] = m.x; uy[p] = m.y;
-      gx[p] = 0.0f; gy[p] = 0.0f; gm[p] = 0.0f;
-    }
-    const int passes = (last - first + 31) >> 5;
-    for (int base = 0; base < total; base += 32) {
-      __syncwarp();
-      {
-        const int s = base + lane;
-        float4 q = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-        float2 m = make_float2(0.0f, 0.0f);
-        if (s < total) {
-          const int g = (s < l0) ? s0 + s : (s < l0 + l1) ? s1 + (s - l0) : s2 + (s - l0 - l1);
-          q = a.sorted4[g];
-          m = a.smu[g];
-        }
-        sl.p[lane] = q;
-        sl.mu[lane] = m;
-      }
-      __syncwarp();
-      const int here = min(32, total - base);
-      for (int k = 0; k < here; ++k) {
-        const float4 q = sl.p[k];
-        const float2 mj = sl.mu[k];
-#pragma unroll
-        for (int p = 0; p < kP2PPasses; ++p) {
-          if (p < passes) {
-            const float dx = q.x - tx[p], dy = q.y - ty[p];
-            const float r2 = fmaf(dy, dy, dx * dx);
-            const float r = sqrt_approx(r2);
-            const float inv = rcp_approx(fmaf(r2, r, eps));
-            // both products rounded: the self pair (d = 0, M = I/eps) then cancels exactly
-            const float vx = __fsub_rn(__fmul_rn(tm[p], mj.x), __fmul_rn(q.z, ux[p]));
-            const float vy = __fsub_rn(__fmul_rn(tm[p], mj.y), __fmul_rn(q.z, uy[p]));
-            const float k3 = 3.0f * r * inv * inv * fmaf(dy, vy, dx * vx);
-            gx[p] = fmaf(vx, inv, fmaf(-k3, dx, gx[p]));
-            gy[p] = fmaf(vy, inv, fmaf(-k3, dy, gy[p]));
-            gm[p] = fmaf(-fmaf(mj.y, dy, mj.x * dx), inv, gm[p]);
-          }
-        }
-      }
-    }
-#pragma unroll
-    for (int p = 0; p < kP2PPasses; ++p) {
-      const int j = first + p * 32 + lane;
-      if (j < last) {
-        float rx = gx[p], ry = gy[p], rm = gm[p];
-        if (a.cell0) {  // transposed P2M of the far field
-          const float4 c = a.cell0[cell];
-          const float4 g = a.g0[cell];
-          if (c.z != 0.0f) {
-            rx += (tm[p] / c.z) * g.x;
-            ry += (tm[p] / c.z) * g.y;
-            rm += g.z + (g.x * (tx[p] - c.x) + g.y * (ty[p] - c.y)) / c.z;
-          }
-        }
-        const int orig = __float_as_int(a.sorted4[j].w);
-        a.gx_out[orig] = make_float2(rx, ry);
-        a.gm_out[orig] = rm;
-      }
+    switch ((last - first + 31) >> 5) {
+      case 1: adj_item<0, 1>(a, sl, lane, cell, first, last, rg); break;
+      case 2: adj_item<1, 0>(a, sl, lane, cell, first, last, rg); break;
+      case 3: adj_item<1, 1>(a, sl, lane, cell, first, last, rg); break;
+      default: adj_item<2, 0>(a, sl, lane, cell, first, last, rg); break;
     }
   }
 }
@@ -439,7 +561,7 @@ struct nbfmm_adjoint {
     a.gx_out = gx;
     a.gm_out = gm;
     cudaMemsetAsync(v.d_work_next(), 0, sizeof(int), s);
-    adj_p2p_kernel<<<v.num_sms * 8, kAdjWarps * 32, 0, s>>>(a);
+    adj_p2p_kernel<<<v.num_sms * 4, kAdjWarps * 32, 0, s>>>(a);
   }
 
   int backward(const float* target, float* grad_x0, float* grad_v0, float* grad_m, cudaStream_t s) {
