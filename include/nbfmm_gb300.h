@@ -165,6 +165,45 @@ int nbfmm_adjoint_backward(nbfmm_adjoint* adj, const float* gpuptr_target, float
                            float* gpuptr_grad_velocity0, float* gpuptr_grad_weight, float* gpuptr_loss_terms,
                            void* stream);
 
+/* ---- Initial-condition models ---------------------------------------------------------------------- */
+
+/* The reference's generators (include/nbfmm/model/model.hpp:36-233, the files of source/nbfmm/model) with the same
+ * arguments: center is {x, y}; cur/prev are float2 [n], w float [n]; tick is the Stars tick (tick * sqrt(G)).
+ * Random angles and positions come from curand_init(0, idx, 0) / curand_uniform as in the reference. Calls
+ * Stars::initialize makes: func(args..., tick_, cur, prev, w). */
+int nbfmm_model_circle_center(int num_particle, const float center[2], float radius, float weight,
+                              float center_weight, float tick, float* gpuptr_position_current,
+                              float* gpuptr_position_previous, float* gpuptr_weight, void* stream);   /* circle_center.cu:49-70 */
+int nbfmm_model_circle_uniform_center(int num_particle, const float center[2], float radius, float weight,
+                                      float center_weight, float tick, float* gpuptr_position_current,
+                                      float* gpuptr_position_previous, float* gpuptr_weight,
+                                      void* stream);                                     /* circle_uniform_center.cu:47-66 */
+int nbfmm_model_disk(int num_particle, const float center[2], float radius, float weight, float tick,
+                     float* gpuptr_position_current, float* gpuptr_position_previous, float* gpuptr_weight,
+                     void* stream);                                                      /* disk.cu:62-81 */
+int nbfmm_model_disk_center(int num_particle, const float center[2], float radius, float weight, float center_weight,
+                            float tick, float* gpuptr_position_current, float* gpuptr_position_previous,
+                            float* gpuptr_weight, void* stream);                         /* disk_center.cu:65-83 */
+int nbfmm_model_disk_static(int num_particle, const float center[2], float radius, float weight, float tick,
+                            float* gpuptr_position_current, float* gpuptr_position_previous, float* gpuptr_weight,
+                            void* stream);                                               /* disk_static.cu:56-74 */
+int nbfmm_model_double_disk(int num_particle1, int num_particle2, const float center1[2], const float center2[2],
+                            float radius1, float radius2, float weight, float eccentricity, float tick,
+                            float* gpuptr_position_current, float* gpuptr_position_previous, float* gpuptr_weight,
+                            void* stream);                                               /* double_disk.cu:39-87 */
+int nbfmm_model_double_disk_center(int num_particle1, int num_particle2, const float center1[2],
+                                   const float center2[2], float radius1, float radius2, float weight,
+                                   float center_weight1, float center_weight2, float eccentricity, float tick,
+                                   float* gpuptr_position_current, float* gpuptr_position_previous,
+                                   float* gpuptr_weight, void* stream);                  /* double_disk_center.cu:39-91 */
+int nbfmm_model_rectangle(int num_particle, const float center[2], float width, float height, float max_weight,
+                          float tick, float* gpuptr_position_current, float* gpuptr_position_previous,
+                          float* gpuptr_weight, void* stream);                           /* rectangle.cu:49-66 */
+/* Checking hook (no counterpart in the reference): later model calls on any thread take their draws from this
+ * device array (3 floats per particle; the second disk of a double disk continues after the first) instead of
+ * curand, so that their arithmetic can be compared with a restatement; NULL restores curand. */
+int nbfmm_model_set_uniforms(const float* gpuptr_uniforms);
+
 /* ---- Allocation-free cell sort ---------------------------------------------------------------------- */
 
 /* No counterpart in the reference. The leaf-cell sort of predo (cell keys, stable sort, heads) for callers

@@ -55,6 +55,15 @@ SIGNATURES = {
     "nbfmm_adjoint_set_epsilon": (ctypes.c_int, [_vp, ctypes.c_float]),
     "nbfmm_adjoint_forward": (ctypes.c_int, [_vp, ctypes.c_int, _vp, _vp, _vp, _vp, _vp]),
     "nbfmm_adjoint_backward": (ctypes.c_int, [_vp, _vp, _vp, _vp, _vp, _vp, _vp]),
+    "nbfmm_model_circle_center": (ctypes.c_int, [ctypes.c_int, _c_float_p] + [ctypes.c_float] * 4 + [_vp] * 4),
+    "nbfmm_model_circle_uniform_center": (ctypes.c_int, [ctypes.c_int, _c_float_p] + [ctypes.c_float] * 4 + [_vp] * 4),
+    "nbfmm_model_disk": (ctypes.c_int, [ctypes.c_int, _c_float_p] + [ctypes.c_float] * 3 + [_vp] * 4),
+    "nbfmm_model_disk_center": (ctypes.c_int, [ctypes.c_int, _c_float_p] + [ctypes.c_float] * 4 + [_vp] * 4),
+    "nbfmm_model_disk_static": (ctypes.c_int, [ctypes.c_int, _c_float_p] + [ctypes.c_float] * 3 + [_vp] * 4),
+    "nbfmm_model_double_disk": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, _c_float_p, _c_float_p] + [ctypes.c_float] * 5 + [_vp] * 4),
+    "nbfmm_model_double_disk_center": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, _c_float_p, _c_float_p] + [ctypes.c_float] * 7 + [_vp] * 4),
+    "nbfmm_model_rectangle": (ctypes.c_int, [ctypes.c_int, _c_float_p] + [ctypes.c_float] * 4 + [_vp] * 4),
+    "nbfmm_model_set_uniforms": (ctypes.c_int, [_vp]),
     "nbfmm_sort_cells_noalloc": (ctypes.c_int, [ctypes.c_int, _c_float_p, ctypes.c_int, _vp, _vp, _vp, _vp]),
     "nbfmm_stars_profile_begin": (ctypes.c_int, [_vp, ctypes.c_int]),
     "nbfmm_stars_profile_end": (ctypes.c_int, [_vp, _c_float_p, _c_int_p]),

@@ -15,6 +15,7 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libnbfmm_gb300.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall",
+              "-Xcompiler", "-ffp-contract=off",  # host arithmetic rounds the same on x86 and Arm
               "--expt-relaxed-constexpr", "-Xptxas", "-warn-spills"]
 
 

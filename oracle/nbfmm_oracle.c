@@ -732,3 +732,122 @@ double orc_traj_direct64_grad(int n, double eps, double tau, int steps, const do
   free(xs); free(xp); free(a); free(l1); free(l2); free(g); free(gmv);
   return loss;
 }
+
+/* ---- Initial-condition models (the files of source/nbfmm/model), given the uniform draws --------------------------- */
+
+static const double kOrcPi = 3.14159265358979323846;
+
+/* kernelFunction(0, (r, 0), m).x with the reference's fixed eps 0.1 (kernel_function.hpp:29-40). */
+static float model_effect_x(float r, float m) {
+  const float rr = sqrtf(r * r + 0.0f * 0.0f);
+  const float tmp = m / (rr * rr * rr + 0.1f);
+  return r * tmp;
+}
+
+/* acos(1.0 - a t t / r / 2): float chain, double subtraction and acos (disk.cu:51). */
+static float model_angle_step(float ax, float tick, float r) {
+  const float q = ax * tick * tick / r / 2.0f;
+  return (float)acos(1.0 - (double)q);
+}
+
+static float model_two_pi_u(float u) { return (float)(2.0 * kOrcPi * (double)u); }
+
+static void model_place(float* cur, float* prev, int i, float cx, float cy, float r, float a, float ap) {
+  cur[2 * i] = fmaf(r, cosf(a), cx);
+  cur[2 * i + 1] = fmaf(r, sinf(a), cy);
+  prev[2 * i] = fmaf(r, cosf(ap), cx);
+  prev[2 * i + 1] = fmaf(r, sinf(ap), cy);
+}
+
+/* circle_center.cu:24-70 (evenly = 0) and circle_uniform_center.cu:24-66 (evenly = 1); u has 3 draws/particle. */
+void orc_model_circle(int n, float cx, float cy, float radius, float weight, float center_weight, float tick,
+                      int evenly, const float* u, float* cur, float* prev, float* w) {
+  const float dangle = model_angle_step(model_effect_x(radius, center_weight), tick, radius);
+  for (int i = 0; i < n; ++i) {
+    if (i == 0) {
+      cur[0] = prev[0] = cx;
+      cur[1] = prev[1] = cy;
+      w[0] = center_weight;
+      continue;
+    }
+    const float a = evenly ? (float)((2.0 * kOrcPi * (double)i) / (double)n) : model_two_pi_u(u[3 * i]);
+    model_place(cur, prev, i, cx, cy, radius, a, a - dangle);
+    w[i] = weight;
+  }
+}
+
+/* disk.cu:30-81 (center = 0), disk_center.cu:30-83 (center = 1), disk_static.cu:30-74 (statik = 1). */
+void orc_model_disk(int n, float cx, float cy, float max_radius, float weight, float center_weight, float tick,
+                    int center, int statik, const float* u, float* cur, float* prev, float* w) {
+  for (int i = 0; i < n; ++i) {
+    if (center && i == 0) {
+      cur[0] = prev[0] = cx;
+      cur[1] = prev[1] = cy;
+      w[0] = center_weight;
+      continue;
+    }
+    const float radius = ((float)(i + 1) / (float)n) * max_radius;
+    float dangle = 0.0f;
+    if (!statik) {
+      const float enclosed = center ? weight * (float)(i - 1) + center_weight : weight * (float)i;
+      dangle = model_angle_step(model_effect_x(radius, enclosed), tick, radius);
+    }
+    const float a = model_two_pi_u(u[3 * i]);
+    model_place(cur, prev, i, cx, cy, radius, a, a - dangle);
+    w[i] = weight;
+  }
+}
+
+/* rectangle.cu:24-66: x, y, then the weight draw. */
+void orc_model_rectangle(int n, float cx, float cy, float width, float height, float max_weight, const float* u,
+                         float* cur, float* prev, float* w) {
+  for (int i = 0; i < n; ++i) {
+    const float x = fmaf(u[3 * i] - 0.5f, width, cx);
+    const float y = fmaf(u[3 * i + 1] - 0.5f, height, cy);
+    cur[2 * i] = prev[2 * i] = x;
+    cur[2 * i + 1] = prev[2 * i + 1] = y;
+    w[i] = max_weight * u[3 * i + 2];
+  }
+}
+
+/* double_disk.cu:58-80: the previous-position offset of disk a in orbit about the common centre. */
+static void model_disk_offset(float ax, float ay, float bx, float by, float mass_b, float ra, float tick, float ecc,
+                              float* ox, float* oy) {
+  float ex, ey;
+  orc_kernel_function(ax, ay, bx, by, mass_b, 0.1f, &ex, &ey);
+  const float a = sqrtf(ex * ex + ey * ey);
+  float x = -ey, y = ex;
+  const float f = sqrtf(ra / a) * tick / exp2f(ecc);
+  x *= f;
+  y *= f;
+  x -= ex * tick * tick * ecc;
+  y -= ey * tick * tick * ecc;
+  *ox = x;
+  *oy = y;
+}
+
+/* double_disk.cu:39-87 (center = 0) and double_disk_center.cu:39-91 (center = 1). */
+void orc_model_double_disk(int n1, int n2, float c1x, float c1y, float c2x, float c2y, float r1, float r2,
+                           float weight, float cw1, float cw2, float ecc, float tick, int center, const float* u,
+                           float* cur, float* prev, float* w) {
+  orc_model_disk(n1, c1x, c1y, r1, weight, cw1, tick, center, 0, u, cur, prev, w);
+  orc_model_disk(n2, c2x, c2y, r2, weight, cw2, tick, center, 0, u + 3 * (size_t)n1, cur + 2 * (size_t)n1,
+                 prev + 2 * (size_t)n1, w + n1);
+  const float m1 = center ? weight * (n1 - 1) + cw1 : weight * n1;
+  const float m2 = center ? weight * (n2 - 1) + cw2 : weight * n2;
+  const float dx = c1x - c2x, dy = c1y - c2y;
+  const float r = sqrtf(dx * dx + dy * dy);
+  const float ra = center ? r * m2 / (m1 + m2) : r * n2 / (n1 + n2);
+  const float rb = center ? r * m1 / (m1 + m2) : r * n1 / (n1 + n2);
+  float o1x, o1y, o2x, o2y;
+  model_disk_offset(c1x, c1y, c2x, c2y, m2, ra, tick, ecc, &o1x, &o1y);
+  model_disk_offset(c2x, c2y, c1x, c1y, m1, rb, tick, ecc, &o2x, &o2y);
+  for (int i = 0; i < n1; ++i) {
+    prev[2 * i] += o1x;
+    prev[2 * i + 1] += o1y;
+  }
+  for (int i = n1; i < n1 + n2; ++i) {
+    prev[2 * i] += o2x;
+    prev[2 * i + 1] += o2y;
+  }
+}

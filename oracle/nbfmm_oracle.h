@@ -104,6 +104,18 @@ double orc_traj_fmm64(int n, int num_level, const float limits[4], double eps, d
 double orc_traj_direct64_grad(int n, double eps, double tau, int steps, const double* x0, const double* v0,
                               const double* m, const double* target, double* gx0, double* gv0, double* gm);
 
+/* The reference's initial-condition models (the files of source/nbfmm/model) for given uniform draws u (3 per particle;
+ * the second disk of a double disk continues after the first). cur/prev float2 [n], w [n]. */
+void orc_model_circle(int n, float cx, float cy, float radius, float weight, float center_weight, float tick,
+                      int evenly, const float* u, float* cur, float* prev, float* w);
+void orc_model_disk(int n, float cx, float cy, float max_radius, float weight, float center_weight, float tick,
+                    int center, int statik, const float* u, float* cur, float* prev, float* w);
+void orc_model_rectangle(int n, float cx, float cy, float width, float height, float max_weight, const float* u,
+                         float* cur, float* prev, float* w);
+void orc_model_double_disk(int n1, int n2, float c1x, float c1y, float c2x, float c2y, float r1, float r2,
+                           float weight, float cw1, float cw2, float ecc, float tick, int center, const float* u,
+                           float* cur, float* prev, float* w);
+
 /* Number of OpenMP threads the oracle will use. */
 int orc_num_threads(void);
 

@@ -50,6 +50,10 @@ def lib():
             "orc_direct_f64": (None, [c_int, _f, _f, ctypes.c_double, ctypes.c_void_p, c_int, _d]),
             "orc_p2p_pairs": (ctypes.c_longlong, [c_int, _i]),
             "orc_num_threads": (c_int, []),
+            "orc_model_circle": (None, [c_int] + [c_float] * 6 + [c_int, _f, _f, _f, _f]),
+            "orc_model_disk": (None, [c_int] + [c_float] * 6 + [c_int, c_int, _f, _f, _f, _f]),
+            "orc_model_rectangle": (None, [c_int] + [c_float] * 5 + [_f, _f, _f, _f]),
+            "orc_model_double_disk": (None, [c_int, c_int] + [c_float] * 11 + [c_int, _f, _f, _f, _f]),
             "orc_traj_fmm64": (ctypes.c_double, [c_int, c_int, _f, ctypes.c_double, ctypes.c_double, c_int, _d, _d, _d,
                                                  ctypes.c_void_p, ctypes.c_void_p, _d, ctypes.c_void_p]),
             "orc_traj_direct64_grad": (ctypes.c_double, [c_int, ctypes.c_double, ctypes.c_double, c_int, _d, _d, _d, _d,
@@ -226,3 +230,27 @@ def traj_direct64_grad(x0, v0, m, eps, tau, steps, target):
     loss = lib().orc_traj_direct64_grad(n, float(eps), float(tau), steps, f64(x0).reshape(-1), f64(v0).reshape(-1),
                                         f64(m), f64(target).reshape(-1), gx, gv, gm)
     return loss, gx.reshape(n, 2), gv.reshape(n, 2), gm
+
+
+def model(kind, n, u, **p):
+    """CPU restatement of one reference model for draws u (n x 3, float32); returns (cur, prev, w)."""
+    total = n if kind not in ("double_disk", "double_disk_center") else p["n1"] + p["n2"]
+    cur = np.zeros((total, 2), np.float32)
+    prev = np.zeros((total, 2), np.float32)
+    w = np.zeros(total, np.float32)
+    uu = f32(u).reshape(-1)
+    L = lib()
+    if kind in ("circle_center", "circle_uniform_center"):
+        L.orc_model_circle(n, *p["center"], p["radius"], p["weight"], p["center_weight"], p["tick"],
+                           int(kind == "circle_uniform_center"), uu, cur, prev, w)
+    elif kind in ("disk", "disk_center", "disk_static"):
+        L.orc_model_disk(n, *p["center"], p["radius"], p["weight"], p.get("center_weight", 0.0), p["tick"],
+                         int(kind == "disk_center"), int(kind == "disk_static"), uu, cur, prev, w)
+    elif kind == "rectangle":
+        L.orc_model_rectangle(n, *p["center"], p["width"], p["height"], p["max_weight"], uu, cur, prev, w)
+    else:
+        center = kind == "double_disk_center"
+        L.orc_model_double_disk(p["n1"], p["n2"], *p["center1"], *p["center2"], p["radius1"], p["radius2"],
+                                p["weight"], p.get("center_weight1", 0.0), p.get("center_weight2", 0.0),
+                                p["eccentricity"], p["tick"], int(center), uu, cur, prev, w)
+    return cur, prev, w
