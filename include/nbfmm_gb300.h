@@ -165,6 +165,41 @@ int nbfmm_adjoint_backward(nbfmm_adjoint* adj, const float* gpuptr_target, float
                            float* gpuptr_grad_velocity0, float* gpuptr_grad_weight, float* gpuptr_loss_terms,
                            void* stream);
 
+/* Stars::prune (prune.cu:28-62) on the public arrays: the stars inside the position limits first, in order, then
+ * the others, in order; num_star becomes the number kept. No host synchronisation. */
+int nbfmm_stars_prune(nbfmm_stars* stars, void* stream);
+
+/* ---- Frames and the .y4m movie ----------------------------------------------------------------------- */
+
+typedef struct nbfmm_movie nbfmm_movie;
+
+/* Bytes of one YUV 4:2:0 frame, width*height*3/2 (main.cu:234). */
+long long nbfmm_frame_bytes(int width, int height);
+
+/* The raster of Stars::display (display.cu:29-221) for any device arrays: clears the frame (Y plane 0, the next
+ * width*height/2 bytes 128) and draws stars [0, num_star) of gpuptr_position (float2) and gpuptr_weight inside
+ * display_limits {x_min, y_min, x_max, y_max}. gpuptr_board holds nbfmm_frame_bytes(width, height) bytes.
+ * The reference's pixels bit for bit, except that writes which would fall outside the frame are dropped (the
+ * reference writes before its buffer for stars on the top rows). */
+int nbfmm_display(int num_star, int width, int height, float size_scale, const float display_limits[4],
+                  const float* gpuptr_position, const float* gpuptr_weight, unsigned char* gpuptr_board,
+                  void* stream);
+
+/* Stars::display(board) (display.cu:219-229): the frame of the current stars, then Stars::prune. width, height,
+ * size_scale and display_limits are the display arguments of the reference's Stars constructor
+ * (stars.hpp:90-92, checked as stars.cu:37-43 asserts them). Use the stream of nbfmm_stars_update. */
+int nbfmm_stars_display(nbfmm_stars* stars, int width, int height, float size_scale, const float display_limits[4],
+                        unsigned char* gpuptr_board, void* stream);
+
+/* The movie of main.cu:228-259: a .y4m file ("YUV4MPEG2 W H F<fps>:1 Ip A1:1 C420", then "FRAME\n" and the
+ * frame per frame) of Stars::display frames. nbfmm_movie_frame displays the stars into the next frame (pruning
+ * them, as Stars::display does) and queues its copy to the host on `stream`; the file write of a frame happens
+ * in the next nbfmm_movie_frame call, overlapping the GPU work queued in between, or in nbfmm_movie_close. */
+int nbfmm_movie_open(nbfmm_stars* stars, const char* path, int width, int height, int fps, float size_scale,
+                     const float display_limits[4], nbfmm_movie** out);
+int nbfmm_movie_frame(nbfmm_movie* movie, void* stream);
+int nbfmm_movie_close(nbfmm_movie* movie);
+
 /* ---- Initial-condition models ---------------------------------------------------------------------- */
 
 /* The reference's generators (include/nbfmm/model/model.hpp:36-233, the files of source/nbfmm/model) with the same

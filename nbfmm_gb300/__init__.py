@@ -17,7 +17,7 @@ import ctypes
 
 from . import _lib
 
-__all__ = ["NbfmmError", "Solver", "Stars", "Batch", "load_library"]
+__all__ = ["NbfmmError", "Solver", "Stars", "Batch", "Movie", "display", "frame_bytes", "load_library"]
 
 
 class NbfmmError(RuntimeError):
@@ -37,7 +37,7 @@ def _check(rc: int):
         raise NbfmmError(rc, _lib.load().nbfmm_last_error().decode())
 
 
-def _ptr(x):
+def _ptr(x, dtype: str = "float32"):
     if x is None:
         return None
     if isinstance(x, int):
@@ -48,8 +48,8 @@ def _ptr(x):
         raise TypeError("expected a torch CUDA tensor or a device address")
     if not x.is_cuda:
         raise ValueError("tensor must live on the GPU")
-    if x.dtype != torch.float32:
-        raise TypeError(f"tensor must be float32, got {x.dtype}")
+    if x.dtype != getattr(torch, dtype):
+        raise TypeError(f"tensor must be {dtype}, got {x.dtype}")
     if not x.is_contiguous():
         raise ValueError("tensor must be contiguous")
     return x.data_ptr()
@@ -181,8 +181,9 @@ class Stars:
     """nbfmm::Stars (include/nbfmm/display/stars.hpp:22-134), update path.
 
     Accepts the reference's constructor arguments (fmm_level, num_star, width, height, fps, tick, grav_const,
-    size_scale, position_limits, display_limits); the display-only ones are checked as the reference asserts
-    them and otherwise unused. `epsilon` is the kernel softening (the reference fixes 1e-1).
+    size_scale, position_limits, display_limits); the display ones are used by display() and checked as the
+    reference asserts them. display_limits defaults to position_limits. `epsilon` is the kernel softening (the
+    reference fixes 1e-1).
     """
 
     def __init__(self, fmm_level, num_star, width=1, height=1, fps=1, tick=None, grav_const=1.0, size_scale=1.0,
@@ -198,7 +199,12 @@ class Stars:
         self._h = h
         self.fmm_level = int(fmm_level)
         self.position_limits = tuple(float(v) for v in position_limits)
-        self.display_limits = display_limits
+        self.display_limits = tuple(float(v) for v in (display_limits if display_limits is not None
+                                                        else position_limits))
+        if not (self.display_limits[0] < self.display_limits[2] and self.display_limits[1] < self.display_limits[3]):
+            raise ValueError("display limits must satisfy x_min < x_max, y_min < y_max (stars.cu:43)")
+        self.width_, self.height_, self.fps_ = int(width), int(height), int(fps)
+        self.size_scale_ = float(size_scale)
         self.max_num_star = int(num_star)
         import numpy as np
 
@@ -249,6 +255,16 @@ class Stars:
     def update(self, num_steps: int = 1, stream=None):
         """`num_steps` x Stars::update() (update.cu:47-55) without host synchronisation."""
         _check(_lib.load().nbfmm_stars_update(self._h, int(num_steps), _stream(stream)))
+
+    def prune(self, stream=None):
+        """Stars::prune (prune.cu:28-62) on the public arrays."""
+        _check(_lib.load().nbfmm_stars_prune(self._h, _stream(stream)))
+
+    def display(self, board, stream=None):
+        """Stars::display(board) (display.cu:219-229): draw the frame (uint8 CUDA tensor or device address of
+        frame_bytes(width, height) bytes), then prune."""
+        _check(_lib.load().nbfmm_stars_display(self._h, self.width_, self.height_, self.size_scale_,
+                                               _limits(self.display_limits), _ptr(board, "uint8"), _stream(stream)))
 
     # Engine instrumentation (no reference counterpart).
     def profile_begin(self, max_steps: int):
@@ -347,3 +363,49 @@ class Batch:
         out = ctypes.c_longlong()
         _check(_lib.load().nbfmm_batch_kernel_launches(self._h, int(num_steps), ctypes.byref(out)))
         return int(out.value)
+
+
+def frame_bytes(width: int, height: int) -> int:
+    """Bytes of one YUV 4:2:0 frame, width*height*3/2 (main.cu:234)."""
+    return int(_lib.load().nbfmm_frame_bytes(int(width), int(height)))
+
+
+def display(position, weight, width, height, size_scale, display_limits, board, num_star=None, stream=None):
+    """The raster of Stars::display (display.cu:29-221) for any device arrays: position (n, 2) float32, weight
+    (n,) float32, board uint8 of frame_bytes(width, height) bytes."""
+    n = int(num_star if num_star is not None else (weight.shape[0] if hasattr(weight, "shape") else 0))
+    _check(_lib.load().nbfmm_display(n, int(width), int(height), float(size_scale), _limits(display_limits),
+                                     _ptr(position), _ptr(weight), _ptr(board, "uint8"), _stream(stream)))
+
+
+class Movie:
+    """The .y4m movie of main.cu:228-259 for one Stars: frame() is Stars::display into the next frame (with its
+    prune); the file write of a frame overlaps the GPU work queued before the next frame() or close()."""
+
+    def __init__(self, stars: Stars, path: str):
+        h = ctypes.c_void_p()
+        _check(_lib.load().nbfmm_movie_open(stars._h, str(path).encode(), stars.width_, stars.height_, stars.fps_,
+                                            stars.size_scale_, _limits(stars.display_limits), ctypes.byref(h)))
+        self._h = h
+        self._stars = stars
+
+    def frame(self, stream=None):
+        _check(_lib.load().nbfmm_movie_frame(self._h, _stream(stream)))
+
+    def close(self):
+        if getattr(self, "_h", None) is not None and self._h.value:
+            h, self._h = self._h, None
+            _check(_lib.load().nbfmm_movie_close(h))
+        self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -39,6 +39,15 @@ SIGNATURES = {
     "nbfmm_stars_state": (ctypes.c_int, [_vp, ctypes.POINTER(_vp), ctypes.POINTER(_vp), ctypes.POINTER(_vp)]),
     "nbfmm_stars_num_star": (ctypes.c_int, [_vp, _c_int_p]),
     "nbfmm_stars_update": (ctypes.c_int, [_vp, ctypes.c_int, _vp]),
+    "nbfmm_stars_prune": (ctypes.c_int, [_vp, _vp]),
+    "nbfmm_frame_bytes": (ctypes.c_longlong, [ctypes.c_int, ctypes.c_int]),
+    "nbfmm_display": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_float, _c_float_p, _vp, _vp,
+                                     _vp, _vp]),
+    "nbfmm_stars_display": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, ctypes.c_float, _c_float_p, _vp, _vp]),
+    "nbfmm_movie_open": (ctypes.c_int, [_vp, ctypes.c_char_p, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                        ctypes.c_float, _c_float_p, ctypes.POINTER(_vp)]),
+    "nbfmm_movie_frame": (ctypes.c_int, [_vp, _vp]),
+    "nbfmm_movie_close": (ctypes.c_int, [_vp]),
     "nbfmm_batch_create": (ctypes.c_int, [ctypes.c_int, _c_int_p, _c_int_p, _c_float_p, ctypes.c_float,
                                           ctypes.c_float, ctypes.POINTER(_vp)]),
     "nbfmm_batch_destroy": (ctypes.c_int, [_vp]),

@@ -409,6 +409,24 @@ struct nbfmm_stars {
     launch_export_gather(sc, v.perm, grave_cur, grave_prev, w_by_orig, cur, prev, w, max_n, s);
     return cuda_check("nbfmm_stars_update");
   }
+
+  // Stars::prune (prune.cu:28-62) on the public arrays: the one-bit stable sort of prune.cu:60, with the count
+  // of kept stars (prune.cu:61) left in the device counter. The final-state files serve as scratch: they are
+  // only live inside an update call.
+  void prune(cudaStream_t s) {
+    nbfmm_solver& v = *solver;
+    launch_prune_keys(v.geo, sc, cur, prev, w, v.keys_a, v.vals_a, grave_cur, grave_prev, w_by_orig, max_n, s);
+    v.sort(sc.n_import, 1, s);
+    launch_head(v.skey, sc.n_import, 1, v.head, sc.num_star, s);  // head[1] = number of kept stars
+    launch_export_gather(sc, v.perm, grave_cur, grave_prev, w_by_orig, cur, prev, w, max_n, s);
+  }
+
+  // Stars::display (display.cu:219-229): the frame of the current stars, then prune.
+  int display(int width, int height, float size_scale, const float* limits, uint8_t* board, cudaStream_t s) {
+    launch_display(sc.num_star, 0, max_n, width, height, size_scale, limits, cur, w, board, s);
+    prune(s);
+    return cuda_check("nbfmm_stars_display");
+  }
 };
 
 extern "C" {
@@ -465,6 +483,24 @@ int nbfmm_stars_update(nbfmm_stars* stars, int num_steps, void* stream) {
   if (!stars) return fail(NBFMM_ERR_INVALID, "null stars handle");
   if (num_steps < 0) return fail(NBFMM_ERR_INVALID, "num_steps must be >= 0");
   return stars->update(num_steps, as_stream(stream));
+}
+
+int nbfmm_stars_prune(nbfmm_stars* stars, void* stream) {
+  if (!stars) return fail(NBFMM_ERR_INVALID, "null stars handle");
+  stars->prune(as_stream(stream));
+  return cuda_check("nbfmm_stars_prune");
+}
+
+int nbfmm_stars_display(nbfmm_stars* stars, int width, int height, float size_scale, const float display_limits[4],
+                        uint8_t* gpuptr_board, void* stream) {
+  if (!stars) return fail(NBFMM_ERR_INVALID, "null stars handle");
+  if (width <= 0 || height <= 0) return fail(NBFMM_ERR_INVALID, "width and height must be > 0 (stars.cu:37-38)");
+  if (!(size_scale > 0.0f)) return fail(NBFMM_ERR_INVALID, "size_scale must be > 0 (stars.cu:41)");
+  if (!display_limits || !(display_limits[0] < display_limits[2] && display_limits[1] < display_limits[3])) {
+    return fail(NBFMM_ERR_INVALID, "display limits must satisfy x_min < x_max, y_min < y_max (stars.cu:43)");
+  }
+  if (!gpuptr_board) return fail(NBFMM_ERR_INVALID, "null frame pointer");
+  return stars->display(width, height, size_scale, display_limits, gpuptr_board, as_stream(stream));
 }
 
 int nbfmm_stars_profile_begin(nbfmm_stars* stars, int max_steps) {

@@ -132,6 +132,23 @@ __global__ void export_gather_kernel(StepCounters sc, const uint32_t* __restrict
 
 __global__ void set_int_kernel(int* p, int v) { *p = v; }
 
+__global__ void prune_keys_kernel(Geometry g, StepCounters sc, const float2* __restrict__ cur,
+                                  const float2* __restrict__ prev, const float* __restrict__ w,
+                                  uint32_t* __restrict__ keys, uint32_t* __restrict__ vals,
+                                  float2* __restrict__ tmp_cur, float2* __restrict__ tmp_prev,
+                                  float* __restrict__ tmp_w) {
+  const int n = *sc.num_star;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const float2 c = cur[i];
+    keys[i] = outside(g, c.x, c.y) ? 1u : 0u;  // prune.cu:40-41
+    vals[i] = (uint32_t)i;
+    tmp_cur[i] = c;
+    tmp_prev[i] = prev[i];
+    tmp_w[i] = w[i];
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) *sc.n_import = n;
+}
+
 int grid_for(long long n, int threads, int cap) {
   long long g = (n + threads - 1) / threads;
   if (g < 1) g = 1;
@@ -188,6 +205,13 @@ void launch_export_gather(const StepCounters& sc, const uint32_t* order, const f
                           int max_n, cudaStream_t stream) {
   export_gather_kernel<<<grid_for(max_n, 256, 152 * 16), 256, 0, stream>>>(sc, order, grave_cur, grave_prev, w_by_orig,
                                                                            cur, prev, w);
+}
+
+void launch_prune_keys(const Geometry& g, const StepCounters& sc, const float2* cur, const float2* prev,
+                       const float* w, uint32_t* keys, uint32_t* vals, float2* tmp_cur, float2* tmp_prev,
+                       float* tmp_w, int max_n, cudaStream_t stream) {
+  prune_keys_kernel<<<grid_for(max_n, 256, 152 * 16), 256, 0, stream>>>(g, sc, cur, prev, w, keys, vals, tmp_cur,
+                                                                        tmp_prev, tmp_w);
 }
 
 }  // namespace nbfmm_gb300

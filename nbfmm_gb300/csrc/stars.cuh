@@ -38,4 +38,16 @@ void launch_export_gather(const StepCounters& sc, const uint32_t* order, const f
                           const float2* grave_prev, const float* w_by_orig, float2* cur, float2* prev, float* w,
                           int max_n, cudaStream_t stream);
 
+// Stars::prune on the public arrays (prune.cu:28-62), step 1: n_import = num_star, keys 1 for the stars outside
+// the limits and 0 otherwise, vals the identity, and a copy of the arrays into tmp_* to gather back from.
+void launch_prune_keys(const Geometry& g, const StepCounters& sc, const float2* cur, const float2* prev,
+                       const float* w, uint32_t* keys, uint32_t* vals, float2* tmp_cur, float2* tmp_prev,
+                       float* tmp_w, int max_n, cudaStream_t stream);
+
+// Frame raster of Stars::display (display.cu): clears the frame and draws stars [0, n) where n = *d_n, or n_host
+// when d_n is null (grid sized for max_n).
+void launch_display(const int* d_n, int n_host, int max_n, int width, int height, float size_scale,
+                    const float* limits, const float2* pos, const float* w, uint8_t* board, cudaStream_t s);
+long long frame_bytes(int width, int height);
+
 }  // namespace nbfmm_gb300

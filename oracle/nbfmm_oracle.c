@@ -394,18 +394,10 @@ int orc_solve_targets(int n, int num_level, const float limits[4], float eps, co
 
 /* update.cu:26-55 and prune.cu:28-62. The position update 2x - x_prev + a*tick*tick is evaluated as
  * fmaf(a*tick, tick, 2x - x_prev), the multiply-add the CUDA compiler forms from update.cu:39. */
-int orc_stars_update(int n, int num_level, const float limits[4], float eps, int p2p_block, float tick_scaled,
-                     float* cur, float* prev, float* w, float* acc) {
-  if (orc_solve(n, num_level, limits, eps, p2p_block, cur, w, acc) != 0) return -1;
-  for (int i = 0; i < n; ++i) {
-    for (int d = 0; d < 2; ++d) {
-      const float p = cur[2 * i + d];
-      const float base = 2.0f * p - prev[2 * i + d];
-      cur[2 * i + d] = fmaf(acc[2 * i + d] * tick_scaled, tick_scaled, base);
-      prev[2 * i + d] = p;
-    }
-  }
-  /* prune.cu:40-41 flags, prune.cu:60 stable partition (kept stars first, order preserved). */
+/* Stars::prune (prune.cu:28-62): flag the stars outside the limits (prune.cu:40-41; NaN is kept), then the
+ * stable sort by flag of prune.cu:60, which keeps the survivors first in their order and moves the pruned
+ * ones behind them, also in order. Returns the number of survivors. */
+int orc_prune(int n, const float limits[4], float* cur, float* prev, float* w) {
   int kept = 0;
   float* dead = (float*)malloc(sizeof(float) * 5 * (size_t)(n > 0 ? n : 1));
   int ndead = 0;
@@ -438,6 +430,20 @@ int orc_stars_update(int n, int num_level, const float limits[4], float eps, int
   }
   free(dead);
   return kept;
+}
+
+int orc_stars_update(int n, int num_level, const float limits[4], float eps, int p2p_block, float tick_scaled,
+                     float* cur, float* prev, float* w, float* acc) {
+  if (orc_solve(n, num_level, limits, eps, p2p_block, cur, w, acc) != 0) return -1;
+  for (int i = 0; i < n; ++i) {
+    for (int d = 0; d < 2; ++d) {
+      const float p = cur[2 * i + d];
+      const float base = 2.0f * p - prev[2 * i + d];
+      cur[2 * i + d] = fmaf(acc[2 * i + d] * tick_scaled, tick_scaled, base);
+      prev[2 * i + d] = p;
+    }
+  }
+  return orc_prune(n, limits, cur, prev, w);
 }
 
 /* All-pairs direct sum in FP64, the error reference for every result (demo.cu:59-66 pattern). */
@@ -849,5 +855,68 @@ void orc_model_double_disk(int n1, int n2, float c1x, float c1y, float c2x, floa
   for (int i = n1; i < n1 + n2; ++i) {
     prev[2 * i] += o2x;
     prev[2 * i + 1] += o2y;
+  }
+}
+
+/* ---- Frame raster (source/nbfmm/display/stars/display.cu) ------------------------------------------------ */
+
+/* float -> int as the GPU converts (cvt.rzi.s32.f32): toward zero, saturating, NaN -> 0. The C cast is
+ * undefined out of range and differs between x86 and Arm there. */
+static int display_to_int(float v) {
+  if (v != v) return 0;
+  if (v >= 2147483648.0f) return 2147483647;
+  if (v <= -2147483648.0f) return (-2147483647 - 1);
+  return (int)v;
+}
+
+/* The pixels displayDevice sets around a star (display.cu:53-212), one row per pixel: the size from which it is
+ * drawn, its offset (dx, dy) from the star's pixel, and the guard the reference tests before the write, as
+ * x >= xa && x < width - xb && y >= ya && y < height - yb (xb or yb = -1: no upper test; the centre pixel's own
+ * test, 0 <= x < width and 0 <= y <= height, always holds when these are evaluated). The guards are the
+ * reference's verbatim, including the irregular ones: pixels straight above test only y >= 0
+ * (display.cu:62,90,130,182), and several diagonal ones test a wider margin than their offset needs. */
+static const signed char kDisplayStamp[48][7] = {
+    /* size dx  dy  xa  xb  ya  yb */
+    {1, -1, 0, 1, -1, 0, -1},  {1, 1, 0, 0, 1, 0, -1},   {1, 0, -1, 0, -1, 0, -1}, {1, 0, 1, 0, -1, 0, 1},
+    {2, -1, -1, 1, -1, 1, -1}, {2, -1, 1, 1, -1, 0, 1},  {2, 1, -1, 0, 1, 1, -1},  {2, 1, 1, 0, 1, 0, 1},
+    {3, -2, 0, 2, -1, 0, -1},  {3, 2, 0, 0, 2, 0, -1},   {3, 0, -2, 0, -1, 0, -1}, {3, 0, 2, 0, -1, 0, 2},
+    {4, -2, -1, 2, -1, 1, -1}, {4, -1, -2, 1, -1, 2, -1}, {4, -2, 1, 2, -1, 0, 2}, {4, -1, 2, 1, -1, 0, 2},
+    {4, 2, -1, 0, 2, 1, -1},   {4, 1, -2, 0, 2, 2, -1},  {4, 2, 1, 0, 2, 0, 2},    {4, 1, 2, 0, 2, 0, 2},
+    {5, -3, 0, 3, -1, 0, -1},  {5, 3, 0, 0, 3, 0, -1},   {5, 0, -3, 0, -1, 0, -1}, {5, 0, 3, 0, -1, 0, 3},
+    {5, -2, -2, 2, -1, 2, -1}, {5, -2, 2, 2, -1, 0, 2},  {5, 2, -2, 0, 2, 2, -1},  {5, 2, 2, 0, 2, 0, 2},
+    {6, -3, -1, 3, -1, 1, -1}, {6, -1, -3, 1, -1, 3, -1}, {6, -3, 1, 3, -1, 0, 3}, {6, -1, 3, 1, -1, 0, 3},
+    {6, 3, -1, 0, 3, 1, -1},   {6, 1, -3, 0, 3, 3, -1},  {6, 3, 1, 0, 3, 0, 3},    {6, 1, 3, 0, 3, 0, 3},
+    {7, -4, 0, 4, -1, 0, -1},  {7, 4, 0, 0, 4, 0, -1},   {7, 0, -4, 0, -1, 0, -1}, {7, 0, 4, 0, -1, 0, 4},
+    {7, -3, -2, 3, -1, 2, -1}, {7, -2, -3, 2, -1, 3, -1}, {7, -3, 2, 3, -1, 0, 3}, {7, -2, 3, 2, -1, 0, 3},
+    {7, 3, -2, 0, 3, 2, -1},   {7, 2, -3, 0, 3, 3, -1},  {7, 3, 2, 0, 3, 0, 3},    {7, 2, 3, 0, 3, 0, 3},
+};
+
+/* Stars::display (display.cu:219-229) without its prune: Y plane 0, the next width*height/2 bytes 128
+ * (display.cu:220-221), then displayDevice (display.cu:29-214) per star. Differences from the reference:
+ * writes that would land outside the frame of width*height*3/2 bytes are dropped (the reference writes before
+ * the buffer for a star on the top rows, through the y >= 0 guards, which is undefined); everything inside the
+ * frame is the reference's, including its acceptance of y == height (display.cu:53), which sets bytes of the
+ * chroma plane that follows the Y plane. */
+void orc_display(int n, int width, int height, float size_scale, const float limits[4], const float* pos,
+                 const float* w, unsigned char* board) {
+  const long long plane = (long long)width * height;
+  const long long frame = plane * 3 / 2;
+  memset(board, 0, (size_t)plane);
+  memset(board + plane, 128, (size_t)(plane / 2));
+  const float unit_width = (limits[2] - limits[0]) / (float)width;    /* display.cu:45 */
+  const float unit_height = (limits[3] - limits[1]) / (float)height;  /* display.cu:46 */
+  for (int i = 0; i < n; ++i) {
+    const int x = display_to_int(floorf((pos[2 * i] - limits[0]) / unit_width));      /* display.cu:47 */
+    const int y = display_to_int(floorf((limits[3] - pos[2 * i + 1]) / unit_height));  /* display.cu:48 */
+    const int size = display_to_int(floorf(sqrtf(w[i]) / size_scale));                 /* display.cu:49 */
+    if (!(0 <= x && x < width && 0 <= y && y <= height)) continue;                      /* display.cu:53 */
+    const long long at = (long long)y * width + x;
+    if (at < frame) board[at] = 255;
+    for (int k = 0; k < 48 && kDisplayStamp[k][0] <= size; ++k) {
+      const signed char* e = kDisplayStamp[k];
+      if (!(x >= e[3] && x < width - e[4] && y >= e[5] && y < height - e[6])) continue;
+      const long long t = at + (long long)e[2] * width + e[1];
+      if (t >= 0 && t < frame) board[t] = 255;
+    }
   }
 }

@@ -80,6 +80,9 @@ int orc_solve(int n, int num_level, const float limits[4], float eps, int p2p_bl
 int orc_solve_targets(int n, int num_level, const float limits[4], float eps, const float* pos, const float* w,
                       const int* targets, int n_targets, float* eff);
 
+/* Stars::prune (prune.cu:28-62): stable partition, stars inside the limits first. Returns the survivors. */
+int orc_prune(int n, const float limits[4], float* cur, float* prev, float* w);
+
 /* One Stars::update (update.cu:47-55): solve, Stormer-Verlet (update.cu:26-42), prune (prune.cu:28-62,
  * stable partition of the stars inside the limits). tick_scaled = tick * sqrt(G) (stars.cu:31).
  * acc receives the solve's effects (pre-update order). Returns the new number of stars. */
@@ -115,6 +118,11 @@ void orc_model_rectangle(int n, float cx, float cy, float width, float height, f
 void orc_model_double_disk(int n1, int n2, float c1x, float c1y, float c2x, float c2y, float r1, float r2,
                            float weight, float cw1, float cw2, float ecc, float tick, int center, const float* u,
                            float* cur, float* prev, float* w);
+
+/* Stars::display without its prune (display.cu:29-229): one YUV 4:2:0 frame of width*height*3/2 bytes.
+ * limits are the display limits [x_min, y_min, x_max, y_max]. Writes outside the frame are dropped. */
+void orc_display(int n, int width, int height, float size_scale, const float limits[4], const float* pos,
+                 const float* w, unsigned char* board);
 
 /* Number of OpenMP threads the oracle will use. */
 int orc_num_threads(void);

@@ -17,6 +17,7 @@ REF_LIB = os.path.join(HERE, "_ref", "libnbfmm_refcpu.so")
 _f = np.ctypeslib.ndpointer(dtype=np.float32, flags="C_CONTIGUOUS")
 _d = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
 _i = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
+_u8 = np.ctypeslib.ndpointer(dtype=np.uint8, flags="C_CONTIGUOUS")
 _lib = None
 
 
@@ -46,6 +47,8 @@ def lib():
             "orc_postdo": (None, [c_int, _i, _f, _f]),
             "orc_solve": (c_int, [c_int, c_int, _f, c_float, c_int, _f, _f, _f]),
             "orc_solve_targets": (c_int, [c_int, c_int, _f, c_float, _f, _f, _i, c_int, _f]),
+            "orc_prune": (c_int, [c_int, _f, _f, _f, _f]),
+            "orc_display": (None, [c_int, c_int, c_int, c_float, _f, _f, _f, _u8]),
             "orc_stars_update": (c_int, [c_int, c_int, _f, c_float, c_int, c_float, _f, _f, _f, _f]),
             "orc_direct_f64": (None, [c_int, _f, _f, ctypes.c_double, ctypes.c_void_p, c_int, _d]),
             "orc_p2p_pairs": (ctypes.c_longlong, [c_int, _i]),
@@ -205,7 +208,46 @@ def ref_lib():
     L.ref_int2_equal.restype = ctypes.c_int
     L.ref_weighted_position.argtypes = [ctypes.c_int, _f, _f, _f]
     L.ref_weighted_position.restype = None
+    L.ref_has_display.argtypes = []
+    L.ref_has_display.restype = ctypes.c_int
+    if L.ref_has_display():
+        L.ref_display_device.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_float, _f, _f, _f, _u8]
+        L.ref_display_device.restype = None
     return L
+
+
+def frame_bytes(width, height):
+    return width * height * 3 // 2
+
+
+def display(pos, w, width, height, size_scale, limits):
+    """Stars::display without its prune: one YUV 4:2:0 frame (uint8, width*height*3/2 bytes)."""
+    pos = f32(pos).reshape(-1)
+    board = np.empty(frame_bytes(width, height), np.uint8)
+    lib().orc_display(len(pos) // 2, width, height, float(size_scale), lim(limits), pos, f32(w), board)
+    return board
+
+
+def ref_display(pos, w, width, height, size_scale, limits, pad_rows=8):
+    """The reference's displayDevice compiled for the CPU (oracle/_ref), on a frame cleared as
+    Stars::display clears it; returns (frame, bytes written before it, bytes written after it), or None."""
+    L = ref_lib()
+    if L is None or not L.ref_has_display():
+        return None
+    pad = pad_rows * width + 8
+    fb = frame_bytes(width, height)
+    buf = np.full(pad + fb + pad, 7, np.uint8)
+    buf[pad:pad + width * height] = 0
+    buf[pad + width * height:pad + fb] = 128
+    pos = f32(pos).reshape(-1)
+    view = buf[pad:]
+    L.ref_display_device(len(pos) // 2, width, height, float(size_scale), lim(limits), pos, f32(w), view)
+    return buf[pad:pad + fb].copy(), int(np.count_nonzero(buf[:pad] != 7)), int(np.count_nonzero(buf[pad + fb:] != 7))
+
+
+def prune(cur, prev, w, limits):
+    """Stars::prune: stable partition in place; returns the number of survivors."""
+    return lib().orc_prune(len(w), lim(limits), cur.reshape(-1), prev.reshape(-1), w)
 
 
 def f64(a):

@@ -9,6 +9,7 @@ if ROOT not in sys.path:
     sys.path.insert(0, ROOT)
 
 GOLDEN = os.path.join(ROOT, "tests", "golden", "ref_fixture_l3_n250.npz")
+DISPLAY_GOLDEN = os.path.join(ROOT, "tests", "golden", "ref_display_frames.npz")
 
 
 def pytest_configure(config):
@@ -19,6 +20,20 @@ def pytest_configure(config):
 def golden():
     d = np.load(GOLDEN)
     return {k: d[k] for k in d.files}
+
+
+@pytest.fixture(scope="session")
+def display_golden():
+    """Frames drawn by the reference's displayDevice: a list of dicts (pos, w, width, height, size_scale, limits,
+    frame)."""
+    d = np.load(DISPLAY_GOLDEN)
+    cases = []
+    for k in range(int(d["num_cases"])):
+        width, height = (int(v) for v in d[f"case{k}_params"])
+        f = d[f"case{k}_fparams"]
+        cases.append(dict(pos=d[f"case{k}_pos"], w=d[f"case{k}_w"], width=width, height=height,
+                          size_scale=float(f[0]), limits=tuple(float(v) for v in f[1:]), frame=d[f"case{k}_frame"]))
+    return cases
 
 
 @pytest.fixture(scope="session")

@@ -194,3 +194,62 @@ def test_cell_index_clamps_the_upper_edge(orc):
     r = orc.predo(pos, np.ones(4, np.float32), 1, (-1, -1, 1, 1))
     idx = r["index"][np.argsort(r["perm"])]
     np.testing.assert_array_equal(idx, [[3, 3], [0, 0], [3, 0], [2, 2]])
+
+
+def test_display_matches_reference_golden_frames(display_golden, orc):
+    """orc_display against frames drawn by the reference's own displayDevice (tests/golden)."""
+    for c in display_golden:
+        frame = orc.display(c["pos"], c["w"], c["width"], c["height"], c["size_scale"], c["limits"])
+        assert frame.shape == c["frame"].shape
+        np.testing.assert_array_equal(frame, c["frame"])
+
+
+def test_display_matches_reference_library(orc):
+    """orc_display against the reference's displayDevice compiled for the CPU (oracle/_ref), random fields."""
+    L = orc.ref_lib()
+    if L is None or not L.ref_has_display():
+        pytest.skip("oracle/_ref was not built from the reference sources")
+    rng = np.random.default_rng(7)
+    for trial in range(25):
+        width, height = int(rng.integers(1, 80)), int(rng.integers(1, 60))
+        size_scale = float(rng.choice([0.1, 0.5, 1.0, 3.0]))
+        limits = (-1.0, -0.5, float(rng.uniform(0.1, 2)), float(rng.uniform(0.1, 1)))
+        n = int(rng.integers(0, 400))
+        pos = np.stack([rng.uniform(-1.3, limits[2] + 0.3, n), rng.uniform(-0.8, limits[3] + 0.3, n)], 1)
+        w = (rng.uniform(0, 10, n) * size_scale) ** 2
+        frame = orc.display(pos, w, width, height, size_scale, limits)
+        ref = orc.ref_display(pos, w, width, height, size_scale, limits)[0]
+        np.testing.assert_array_equal(frame, ref, err_msg=f"trial {trial}: {width}x{height}")
+
+
+def test_display_special_values(orc):
+    """NaN, infinite and huge coordinates and weights convert as the GPU converts (saturating, NaN -> 0)."""
+    pos = np.array([[np.nan, 0.0], [0.0, np.nan], [np.inf, 0.0], [-np.inf, 0.0], [1e30, 0.0], [0.0, -1e30],
+                    [-0.75, -0.75]], np.float32)
+    w = np.array([1.0, 1.0, 1.0, 1.0, 1.0, 1.0, -4.0], np.float32)
+    frame = orc.display(pos, w, 8, 8, 1.0, (-1, -1, 1, 1))
+    y = frame[:64].reshape(8, 8)
+    lit = {(int(r), int(c)) for r, c in zip(*np.nonzero(y))}
+    # NaN x -> column 0, row 4, size 1 (its left pixel is guarded); NaN y -> row 0, column 4 (the pixel above it
+    # would be before the frame and is dropped); +-inf and 1e30 saturate off the frame; the negative weight
+    # gives size floor(NaN) -> 0, the centre pixel alone (row 7, column 1).
+    assert lit == {(4, 0), (4, 1), (3, 0), (5, 0), (0, 4), (0, 3), (0, 5), (1, 4), (7, 1)}
+    assert np.all(frame[64:] == 128)
+
+
+def test_prune_is_a_stable_partition(orc):
+    rng = np.random.default_rng(3)
+    n = 5000
+    cur = rng.uniform(-1.5, 1.5, (n, 2)).astype(np.float32)
+    cur[::97] = np.nan  # NaN is kept (the comparisons of prune.cu:40-41 are false)
+    prev = rng.normal(size=(n, 2)).astype(np.float32)
+    w = rng.uniform(size=n).astype(np.float32)
+    limits = (-1.0, -1.0, 1.0, 1.0)
+    out = (cur[:, 0] < -1) | (cur[:, 1] < -1) | (cur[:, 0] > 1) | (cur[:, 1] > 1)
+    order = np.concatenate([np.flatnonzero(~out), np.flatnonzero(out)])
+    ec, ep, ew = cur[order].copy(), prev[order].copy(), w[order].copy()
+    kept = orc.prune(cur, prev, w, limits)
+    assert kept == int((~out).sum())
+    np.testing.assert_array_equal(cur, ec)
+    np.testing.assert_array_equal(prev, ep)
+    np.testing.assert_array_equal(w, ew)
