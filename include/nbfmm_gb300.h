@@ -252,6 +252,16 @@ int nbfmm_model_set_uniforms(const float* gpuptr_uniforms);
 int nbfmm_sort_cells_noalloc(int num_level, const float position_limits[4], int num_particle,
                              const float* gpuptr_position, int* gpuptr_perm, int* gpuptr_head, void* stream);
 
+/* ---- Device memory for hosts that link only this library ------------------------------------------- */
+
+/* cudaMalloc, cudaFree and synchronous cudaMemcpy through this library's CUDA runtime, for C hosts (the
+ * command-line programs, a cgo or ctypes binding) that do not link the CUDA runtime themselves. The reference's
+ * programs call the runtime directly for these (demo.cu:43-45, 69-72, 94-96). */
+int nbfmm_device_malloc(unsigned long long bytes, void** gpuptr_out);
+int nbfmm_device_free(void* gpuptr);
+int nbfmm_memcpy_to_device(void* gpuptr_dst, const void* src, unsigned long long bytes);
+int nbfmm_memcpy_to_host(void* dst, const void* gpuptr_src, unsigned long long bytes);
+
 /* ---- Instrumentation (engine-only; the reference has no timing, no events, no counters) ------------ */
 
 /* Times the P2P launch of each of the next `max_steps` update steps with a pair of CUDA events recorded

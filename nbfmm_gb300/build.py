@@ -1,7 +1,9 @@
-"""Builds libnbfmm_gb300.so in-tree from nbfmm_gb300/csrc/*.cu for sm_103a (GB300).
+"""Builds libnbfmm_gb300.so in-tree from nbfmm_gb300/csrc/*.cu for sm_103a (GB300), and the command-line
+programs nbfmm_gb300/bin/nbfmm_main and nbfmm_demo from nbfmm_gb300/cli/*.cpp.
 
 Each translation unit is compiled in parallel with nvcc, then linked into one shared library with the CUDA
-runtime linked statically. `python -m nbfmm_gb300.build` or `build()` from Python.
+runtime linked statically. The programs are plain C++ on the library's C ABI. `python -m nbfmm_gb300.build`
+or `build()` from Python.
 """
 import concurrent.futures
 import os
@@ -13,6 +15,10 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libnbfmm_gb300.so")
+CLI = os.path.join(HERE, "cli")
+BIN = os.path.join(HERE, "bin")
+INCLUDE = os.path.join(HERE, "..", "include")
+PROGRAMS = {"nbfmm_main": "main.cpp", "nbfmm_demo": "demo.cpp"}
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall",
               "-Xcompiler", "-ffp-contract=off",  # host arithmetic rounds the same on x86 and Arm
@@ -60,7 +66,29 @@ def build(verbose: bool = False, extra_flags=None) -> str:
         if r.returncode != 0:
             sys.stderr.write(" ".join(cmd) + "\n" + r.stdout + r.stderr)
             raise RuntimeError("link of libnbfmm_gb300.so failed")
+    build_programs(verbose)
     return LIB
+
+
+def program(name: str) -> str:
+    return os.path.join(BIN, name)
+
+
+def build_programs(verbose: bool = False):
+    """The command-line programs, linked against the in-tree library (rpath $ORIGIN/..)."""
+    os.makedirs(BIN, exist_ok=True)
+    cxx = os.environ.get("CXX", "g++")
+    for name, src in PROGRAMS.items():
+        out, src = program(name), os.path.join(CLI, src)
+        if not _stale(out, [src, LIB, os.path.join(INCLUDE, "nbfmm_gb300.h")]):
+            continue
+        cmd = [cxx, "-O2", "-std=c++17", "-ffp-contract=off", "-Wall", "-I" + INCLUDE, src, "-o", out,
+               "-L" + HERE, "-lnbfmm_gb300", "-Wl,-rpath,$ORIGIN/.."]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if verbose or r.returncode != 0:
+            sys.stderr.write(" ".join(cmd) + "\n" + r.stdout + r.stderr)
+        if r.returncode != 0:
+            raise RuntimeError(f"build of {name} failed")
 
 
 if __name__ == "__main__":

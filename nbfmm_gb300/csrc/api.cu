@@ -485,6 +485,41 @@ int nbfmm_stars_update(nbfmm_stars* stars, int num_steps, void* stream) {
   return stars->update(num_steps, as_stream(stream));
 }
 
+int nbfmm_device_malloc(unsigned long long bytes, void** gpuptr_out) {
+  if (!gpuptr_out) return fail(NBFMM_ERR_INVALID, "null output pointer");
+  *gpuptr_out = nullptr;
+  if (bytes == 0) return NBFMM_OK;
+  if (cudaMalloc(gpuptr_out, (size_t)bytes) != cudaSuccess) {
+    cudaGetLastError();
+    *gpuptr_out = nullptr;
+    return fail(NBFMM_ERR_NOMEM, "cudaMalloc of %llu bytes failed", bytes);
+  }
+  return NBFMM_OK;
+}
+
+int nbfmm_device_free(void* gpuptr) {
+  if (gpuptr && cudaFree(gpuptr) != cudaSuccess) return cuda_check("cudaFree");
+  return NBFMM_OK;
+}
+
+int nbfmm_memcpy_to_device(void* gpuptr_dst, const void* src, unsigned long long bytes) {
+  if (bytes == 0) return NBFMM_OK;
+  if (!gpuptr_dst || !src) return fail(NBFMM_ERR_INVALID, "null pointer");
+  if (cudaMemcpy(gpuptr_dst, src, (size_t)bytes, cudaMemcpyHostToDevice) != cudaSuccess) {
+    return cuda_check("cudaMemcpy to device");
+  }
+  return NBFMM_OK;
+}
+
+int nbfmm_memcpy_to_host(void* dst, const void* gpuptr_src, unsigned long long bytes) {
+  if (bytes == 0) return NBFMM_OK;
+  if (!dst || !gpuptr_src) return fail(NBFMM_ERR_INVALID, "null pointer");
+  if (cudaMemcpy(dst, gpuptr_src, (size_t)bytes, cudaMemcpyDeviceToHost) != cudaSuccess) {
+    return cuda_check("cudaMemcpy to host");
+  }
+  return NBFMM_OK;
+}
+
 int nbfmm_stars_prune(nbfmm_stars* stars, void* stream) {
   if (!stars) return fail(NBFMM_ERR_INVALID, "null stars handle");
   stars->prune(as_stream(stream));
