@@ -88,3 +88,31 @@ def test_python_mirror_raises_without_the_library(tmp_path):
             _lib.load(str(tmp_path / "missing.so"))
     finally:
         _lib._lib = saved
+
+
+def build_facade_check(out_path):
+    """Compiles tests/cxx/facade_check.cpp against the C++ facade and links it to the library."""
+    import shutil
+    import subprocess
+
+    from nbfmm_gb300 import build
+
+    cxx = shutil.which(os.environ.get("CXX", "g++"))
+    cuda_inc = os.path.join(os.environ.get("CUDA_HOME", "/usr/local/cuda"), "include")
+    if cxx is None or not os.path.exists(os.path.join(cuda_inc, "vector_types.h")):
+        pytest.skip("needs g++ and the CUDA headers")
+    if not os.path.exists(build.LIB):
+        build.build()
+    src = os.path.join(ROOT, "tests", "cxx", "facade_check.cpp")
+    cmd = [cxx, "-std=c++17", "-Wall", "-Werror", "-I" + os.path.join(ROOT, "include"), "-I" + cuda_inc, src,
+           "-o", out_path, "-L" + os.path.dirname(build.LIB), "-lnbfmm_gb300",
+           "-Wl,-rpath," + os.path.dirname(build.LIB)]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    return out_path
+
+
+def test_cxx_facade_compiles_and_links(tmp_path):
+    """include/nbfmm_gb300.hpp: reference-style code (Solver, Stars.initialize with a model, update, display)
+    compiles against the facade and links to the library."""
+    assert os.path.exists(build_facade_check(str(tmp_path / "facade_check")))

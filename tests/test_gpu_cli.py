@@ -124,3 +124,33 @@ def test_demo(programs, orc):
     cpu, fmm = vals[:, 5:7], vals[:, 7:9]
     rel = np.linalg.norm(cpu - fmm, axis=1) / np.linalg.norm(cpu, axis=1).max()
     assert np.median(rel) < 0.05  # the method's own error at depth 4 with monopoles
+
+
+def test_cxx_facade_runs_like_the_python_api(engine, tmp_path):
+    """Reference-style C++ (include/nbfmm_gb300.hpp) gives the numbers the Python API gives for the same run."""
+    import sys
+
+    import torch
+    from nbfmm_gb300 import model
+
+    sys.path.insert(0, os.path.dirname(__file__))
+    from test_abi import build_facade_check
+
+    exe = build_facade_check(str(tmp_path / "facade_check"))
+    r = run(exe)
+    assert r.returncode == 0, r.stderr
+    esum, n_after, lit = r.stdout.split()
+    n = 4096
+    st = engine.Stars(4, n, 64, 48, 30, 1e-3, 1.0, 0.05, (-2, -2, 2, 2), (-1.5, -1.5, 1.5, 1.5))
+    st.initialize(model.generateDiskCenter, n, (0.0, 0.0), 1.0, 1e-4, 5.0)
+    solver = engine.Solver(4, n, (-2, -2, 2, 2))
+    eff = torch.empty(n, 2, device="cuda")
+    solver.solve(n, st.gpuptr_position_cur_, st.gpuptr_weight_, eff)
+    st.update(5)
+    board = torch.empty(engine.frame_bytes(64, 48), dtype=torch.uint8, device="cuda")
+    st.display(board)
+    torch.cuda.synchronize()
+    e = eff.cpu().numpy().astype(np.float64).ravel()
+    assert abs(float(esum) - e.sum()) <= 1e-9 * np.abs(e).sum()
+    assert int(n_after) == st.num_star_
+    assert int(lit) == int((board[:64 * 48] == 255).sum())
