@@ -128,6 +128,39 @@ def run_reference_arm(args, sysm, rank):
     print(json.dumps(out), flush=True)
 
 
+def run_reference_mode(args):
+    """The reference arm of the modes outside the Stars step: the raster has a CPU restatement; the batched form
+    and the adjoint have no counterpart in the reference."""
+    if args.config != "display_16m":
+        why = {"batched_512": "the reference has no batched form (it steps one system per Stars)",
+               "adjoint_262k": "the reference has no adjoint"}.get(args.config, f"unknown config {args.config}")
+        print(json.dumps({"impl": "reference", "unavailable": why}), flush=True)
+        return
+    from nbfmm_gb300 import workloads
+    from oracle import oracle
+
+    oracle.lib()
+    sysm = workloads.two_disks()
+    n, width, height, size_scale = sysm.n, 1920, 1080, 1e-4
+    for _ in range(args.warmup):
+        oracle.display(sysm.position, sysm.weight, width, height, size_scale, sysm.limits, threads=True)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        oracle.display(sysm.position, sysm.weight, width, height, size_scale, sysm.limits, threads=True)
+    el = time.perf_counter() - t0
+    v = n * args.steps / el
+    print(json.dumps({
+        "impl": "reference", "metric": "stars/s", "value": v, "unit": "stars/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": el * 1e3 / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
+        "config": {"workload": f"display: the two-disk state, N={n:,}, into a {width}x{height} YUV 4:2:0 frame",
+                   "parallelism": "host threads"},
+        "cpu_baseline": {"value": v, "unit": "stars/s", "cores": oracle.num_threads(), "kind": "port",
+                         "sample": f"{args.steps} frames of the whole workload"},
+        "e2e": {"value": v, "unit": "stars/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }), flush=True)
+
+
 # ---- GPU side --------------------------------------------------------------------------------------------------
 
 class ClockSampler:
@@ -328,6 +361,111 @@ def run_adjoint(args):
     print(json.dumps(out), flush=True)
 
 
+# DRAM bytes (read + write) of one raster_bits_kernel launch per star, from the ncu capture of the display
+# workload itself (profiles/raster_kernel_two_disks.md: 201.60 MB + 3.42 MB at N = 16,777,216).
+DISPLAY_DRAM_BYTES_PER_STAR = (201.596928e6 + 3.421184e6) / 16777216
+
+
+def run_display(args):
+    """The frame raster of Stars::display (display.cu:29-221): the 16.8M two-disk state drawn into one 1920 x 1080
+    YUV 4:2:0 frame per step. value = stars drawn per second on the device; e2e = the same through the movie
+    writer (raster, prune, frame copy to pinned host memory, file write)."""
+    import tempfile
+
+    import torch
+
+    import nbfmm_gb300
+    from nbfmm_gb300 import workloads
+
+    sysm = workloads.two_disks()
+    n, width, height, size_scale = sysm.n, 1920, 1080, 1e-4
+    lim = sysm.limits
+    pos = torch.from_numpy(sysm.position).cuda()
+    w = torch.from_numpy(sysm.weight).cuda()
+    fb = nbfmm_gb300.frame_bytes(width, height)
+    board = torch.empty(fb, dtype=torch.uint8, device="cuda")
+    stream = torch.cuda.current_stream()
+    for _ in range(max(3, args.warmup)):
+        nbfmm_gb300.display(pos, w, width, height, size_scale, lim, board)
+    torch.cuda.synchronize()
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2 * args.steps)]
+    clocks = ClockSampler("0")
+    t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    t0.record(stream)
+    for k in range(args.steps):
+        ev[2 * k].record(stream)
+        nbfmm_gb300.display(pos, w, width, height, size_scale, lim, board)
+        ev[2 * k + 1].record(stream)
+    t1.record(stream)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    total_ms = t0.elapsed_time(t1)
+    launch_ms = statistics.mean(ev[2 * k].elapsed_time(ev[2 * k + 1]) for k in range(args.steps))
+    lit = int((board[:width * height] == 255).sum())
+
+    # e2e: the movie writer on a Stars holding the same state (its first frame prunes nothing: all stars are
+    # inside the limits).
+    st = nbfmm_gb300.Stars(sysm.num_level, n, width, height, 30, sysm.dt, sysm.grav_const, size_scale, lim, lim,
+                           epsilon=sysm.epsilon)
+    st.gpuptr_position_cur_.copy_(pos)
+    st.gpuptr_position_pre_.copy_(torch.from_numpy(sysm.previous()).cuda())
+    st.gpuptr_weight_.copy_(w)
+    torch.cuda.synchronize()
+    with tempfile.TemporaryDirectory() as tmp:
+        path = os.path.join(tmp, "frames.y4m")
+        with nbfmm_gb300.Movie(st, path) as mv:
+            for _ in range(max(3, args.warmup)):
+                mv.frame()
+            torch.cuda.synchronize()
+            w0 = time.perf_counter()
+            for _ in range(args.steps):
+                mv.frame()
+            mv.close()
+            e2e_s = time.perf_counter() - w0
+        file_bytes = os.path.getsize(path)
+
+    cpu = None
+    if not args.no_cpu_baseline:
+        from oracle import oracle
+
+        oracle.lib()
+        reps = 3
+        c0 = time.perf_counter()
+        for _ in range(reps):
+            ref = oracle.display(sysm.position, sysm.weight, width, height, size_scale, lim, threads=True)
+        cpu_s = (time.perf_counter() - c0) / reps
+        cpu = {"value": n / cpu_s, "unit": "stars/s", "cores": oracle.num_threads(), "kind": "port",
+               "sample": f"the whole workload ({n:,} stars, one 1920x1080 frame), {reps} frames, oracle raster "
+                         "(C, OpenMP over the host cores)",
+               "frame_equal": bool(np.array_equal(ref, board.cpu().numpy()))}
+
+    peak = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))["hbm_gbs"]
+    alg_bytes = 12 * n + fb
+    achieved = alg_bytes / (launch_ms / 1e3) / 1e9
+    out = {
+        "metric": "stars/s", "value": n * args.steps / (total_ms / 1e3), "unit": "stars/s", "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded; nbfmm_gb300/workloads.py)",
+        "config": {"workload": f"display: the two-disk state, N={n:,}, into a {width}x{height} YUV 4:2:0 frame, "
+                               f"size_scale {size_scale:g}, display limits = position limits {list(lim)}",
+                   "l2": "inputs larger than L2 (positions and weights 12 B/star = 201 MB)", "lit_pixels": lit},
+        "roofline": {"kernel": "raster_bits_kernel + expand_kernel (the whole frame)", "bound": "hbm", "unit": "GB/s",
+                     "achieved": achieved, "peak": peak, "frac": achieved / peak,
+                     "traffic": (DISPLAY_DRAM_BYTES_PER_STAR * n if DISPLAY_DRAM_BYTES_PER_STAR else None),
+                     "algorithmic_bytes": alg_bytes, "launch_ms": launch_ms,
+                     "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of raster_bits_kernel on "
+                                       "this workload",
+                     "note": "the raster issues IEEE-exact pixel arithmetic and shared-memory atomics per star; it "
+                             "is bound by SIMT issue, not by HBM",
+                     "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured copy bandwidth)"},
+        "e2e": {"value": n * args.steps / e2e_s, "unit": "stars/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": fb, "api": "Movie.frame(): Stars.display (raster + prune), frame copy to "
+                "pinned host memory, .y4m file write; wall clock", "file_bytes": file_bytes},
+        "cpu_baseline": cpu, "gpu_launches": args.steps, "clocks": clk,
+    }
+    print(json.dumps(out), flush=True)
+
+
 def main():
     args = parse()
     from nbfmm_gb300 import workloads
@@ -336,10 +474,16 @@ def main():
         return run_batched(args)
     if args.config == "adjoint_262k" and args.impl == "gb300":
         return run_adjoint(args)
+    if args.config == "display_16m" and args.impl == "gb300":
+        return run_display(args)
 
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference" and args.config not in workloads.CONFIGS:
+        if rank == 0:
+            run_reference_mode(args)
+        return
     sysm = workloads.CONFIGS[args.config]()
 
     if args.impl == "reference":

@@ -920,3 +920,36 @@ void orc_display(int n, int width, int height, float size_scale, const float lim
     }
   }
 }
+
+/* orc_display over the host threads: each thread draws a slice of the stars into its own frame, and the frames
+ * are merged by maximum. Every write stores 255 over a cleared frame, so the merge equals the sequential raster. */
+void orc_display_threads(int n, int width, int height, float size_scale, const float limits[4], const float* pos,
+                         const float* w, unsigned char* board) {
+  const int threads = omp_get_max_threads();
+  const long long frame = (long long)width * height * 3 / 2;
+  if (threads <= 1 || n < 65536) {
+    orc_display(n, width, height, size_scale, limits, pos, w, board);
+    return;
+  }
+  unsigned char* part = (unsigned char*)malloc((size_t)frame * (size_t)threads);
+  if (!part) {
+    orc_display(n, width, height, size_scale, limits, pos, w, board);
+    return;
+  }
+#pragma omp parallel num_threads(threads)
+  {
+    const int t = omp_get_thread_num();
+    const int lo = (int)((long long)n * t / threads), hi = (int)((long long)n * (t + 1) / threads);
+    orc_display(hi - lo, width, height, size_scale, limits, pos + 2 * (size_t)lo, w + lo, part + (size_t)t * frame);
+  }
+#pragma omp parallel for
+  for (long long i = 0; i < frame; ++i) {
+    unsigned char v = part[i];
+    for (int t = 1; t < threads; ++t) {
+      const unsigned char u = part[(size_t)t * frame + i];
+      v = u > v ? u : v;
+    }
+    board[i] = v;
+  }
+  free(part);
+}

@@ -124,6 +124,10 @@ void orc_model_double_disk(int n1, int n2, float c1x, float c1y, float c2x, floa
 void orc_display(int n, int width, int height, float size_scale, const float limits[4], const float* pos,
                  const float* w, unsigned char* board);
 
+/* orc_display split over the OpenMP threads (per-thread frames merged by maximum); the same frame. */
+void orc_display_threads(int n, int width, int height, float size_scale, const float limits[4], const float* pos,
+                         const float* w, unsigned char* board);
+
 /* Number of OpenMP threads the oracle will use. */
 int orc_num_threads(void);
 

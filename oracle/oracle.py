@@ -49,6 +49,7 @@ def lib():
             "orc_solve_targets": (c_int, [c_int, c_int, _f, c_float, _f, _f, _i, c_int, _f]),
             "orc_prune": (c_int, [c_int, _f, _f, _f, _f]),
             "orc_display": (None, [c_int, c_int, c_int, c_float, _f, _f, _f, _u8]),
+            "orc_display_threads": (None, [c_int, c_int, c_int, c_float, _f, _f, _f, _u8]),
             "orc_stars_update": (c_int, [c_int, c_int, _f, c_float, c_int, c_float, _f, _f, _f, _f]),
             "orc_direct_f64": (None, [c_int, _f, _f, ctypes.c_double, ctypes.c_void_p, c_int, _d]),
             "orc_p2p_pairs": (ctypes.c_longlong, [c_int, _i]),
@@ -220,11 +221,13 @@ def frame_bytes(width, height):
     return width * height * 3 // 2
 
 
-def display(pos, w, width, height, size_scale, limits):
-    """Stars::display without its prune: one YUV 4:2:0 frame (uint8, width*height*3/2 bytes)."""
+def display(pos, w, width, height, size_scale, limits, threads=False):
+    """Stars::display without its prune: one YUV 4:2:0 frame (uint8, width*height*3/2 bytes); threads=True
+    splits the stars over the OpenMP threads (the same frame)."""
     pos = f32(pos).reshape(-1)
     board = np.empty(frame_bytes(width, height), np.uint8)
-    lib().orc_display(len(pos) // 2, width, height, float(size_scale), lim(limits), pos, f32(w), board)
+    fn = lib().orc_display_threads if threads else lib().orc_display
+    fn(len(pos) // 2, width, height, float(size_scale), lim(limits), pos, f32(w), board)
     return board
 
 

@@ -43,6 +43,39 @@ def test_display_matches_oracle_large(engine, orc, n, width, height, size_scale)
     np.testing.assert_array_equal(frame, orc.display(pos, w, width, height, size_scale, limits))
 
 
+@pytest.mark.parametrize("width,height,n", [
+    (3840, 2160, 2_000_000),  # the bitmask raster over 6 bands
+    (6000, 4500, 20_000),     # more bits than 16 shared-memory bands: the byte-store raster
+])
+def test_display_large_frames(engine, orc, width, height, n):
+    rng = np.random.default_rng(width)
+    pos = rng.uniform(-1.05, 1.05, (n, 2)).astype(np.float32)
+    pos[:64, 1] = 1.0 - rng.uniform(0, 3e-3, 64)  # stars on the top rows
+    pos[64:128, 1] = -1.0 - rng.uniform(0, 4e-4, 64)  # and on row `height`
+    w = (rng.uniform(0, 9, n) * 0.01) ** 2
+    frame = gpu_frame(engine, pos, w, width, height, 0.01, (-1, -1, 1, 1))
+    np.testing.assert_array_equal(frame, orc.display(pos, w, width, height, 0.01, (-1, -1, 1, 1)))
+
+
+def test_display_unaligned_frame(engine, orc):
+    """A frame that does not start on a 16-byte boundary takes the byte-wise stores of the expansion."""
+    import torch
+
+    rng = np.random.default_rng(5)
+    n, width, height = 50_000, 200, 120
+    pos = rng.uniform(-1.0, 1.0, (n, 2)).astype(np.float32)
+    w = (rng.uniform(0, 9, n) * 0.01) ** 2
+    fb = engine.frame_bytes(width, height)
+    buf = torch.full((fb + 3,), 7, dtype=torch.uint8, device="cuda")
+    p = torch.from_numpy(pos).cuda()
+    m = torch.from_numpy(w.astype(np.float32)).cuda()
+    engine.display(p, m, width, height, 0.01, (-1, -1, 1, 1), buf.data_ptr() + 3, num_star=n)
+    torch.cuda.synchronize()
+    out = buf.cpu().numpy()
+    assert np.all(out[:3] == 7)
+    np.testing.assert_array_equal(out[3:], orc.display(pos, w, width, height, 0.01, (-1, -1, 1, 1)))
+
+
 def test_display_special_values_and_empty(engine, orc):
     pos = np.array([[np.nan, 0.0], [0.0, np.nan], [np.inf, 0.0], [-np.inf, 0.0], [1e30, 0.0], [0.0, -1e30],
                     [-0.75, -0.75], [0.3, 0.3], [0.999, -0.999], [-1.0, 1.0]], np.float32)

@@ -253,3 +253,13 @@ def test_prune_is_a_stable_partition(orc):
     np.testing.assert_array_equal(cur, ec)
     np.testing.assert_array_equal(prev, ep)
     np.testing.assert_array_equal(w, ew)
+
+
+def test_threaded_display_equals_sequential(orc):
+    rng = np.random.default_rng(11)
+    n = 300_000
+    pos = rng.uniform(-1.1, 1.1, (n, 2)).astype(np.float32)
+    w = (rng.uniform(0, 8, n) * 0.01) ** 2
+    a = orc.display(pos, w, 320, 200, 0.01, (-1, -1, 1, 1))
+    b = orc.display(pos, w, 320, 200, 0.01, (-1, -1, 1, 1), threads=True)
+    np.testing.assert_array_equal(a, b)
