@@ -560,35 +560,59 @@ def main():
     pairs1 = p2p_pairs(torch, solver.buffers()["head"], b)
     pairs = 0.5 * (pairs0 + pairs1)
 
-    # ---- e2e: the public API with host buffers; every step copies the state in and out ----
+    # ---- e2e: the same steps through the public API with host buffers. A second Stars restarts from the initial
+    # state, runs the same warm-up steps untimed, then the same K steps; every step copies the state in from
+    # pinned host memory, runs update(1) and copies the state out. ----
     e2e_steps = args.steps
-    h_cur = torch.empty(n_end, 2, pin_memory=True)
-    h_prev = torch.empty(n_end, 2, pin_memory=True)
-    h_w = torch.empty(n_end, pin_memory=True)
-    h_cur.copy_(stars.gpuptr_position_cur_[:n_end])
-    h_prev.copy_(stars.gpuptr_position_pre_[:n_end])
-    h_w.copy_(stars.gpuptr_weight_[:n_end])
+    st2 = nbfmm_gb300.Stars(sysm.num_level, n, tick=sysm.dt, grav_const=sysm.grav_const,
+                            position_limits=sysm.limits, epsilon=sysm.epsilon)
+    h_cur = torch.empty(n, 2, pin_memory=True)
+    h_prev = torch.empty(n, 2, pin_memory=True)
+    h_w = torch.empty(n, pin_memory=True)
+    h_cur.copy_(pos)
+    h_prev.copy_(prev)
+    h_w.copy_(w)
+    pub = (st2.gpuptr_position_cur_[:n], st2.gpuptr_position_pre_[:n], st2.gpuptr_weight_[:n])
+    host = (h_cur, h_prev, h_w)
+
+    def e2e_step(marks=None):
+        if marks:
+            marks[0].record(stream)
+        for d, h in zip(pub, host):
+            d.copy_(h, non_blocking=True)
+        if marks:
+            marks[1].record(stream)
+        st2.update(1)
+        if marks:
+            marks[2].record(stream)
+        for d, h in zip(pub, host):
+            h.copy_(d, non_blocking=True)
+        if marks:
+            marks[3].record(stream)
+
+    for _ in range(args.warmup):
+        e2e_step()
     torch.cuda.synchronize()
     if dist:
         dist.barrier()
+    parts = [[torch.cuda.Event(enable_timing=True) for _ in range(4)] for _ in range(e2e_steps)]
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e2e_clocks = ClockSampler(dev_id)
     e0.record(stream)
-    for _ in range(e2e_steps):
-        stars.gpuptr_position_cur_[:n_end].copy_(h_cur, non_blocking=True)
-        stars.gpuptr_position_pre_[:n_end].copy_(h_prev, non_blocking=True)
-        stars.gpuptr_weight_[:n_end].copy_(h_w, non_blocking=True)
-        stars.update(1)
-        h_cur.copy_(stars.gpuptr_position_cur_[:n_end], non_blocking=True)
-        h_prev.copy_(stars.gpuptr_position_pre_[:n_end], non_blocking=True)
-        h_w.copy_(stars.gpuptr_weight_[:n_end], non_blocking=True)
+    for k in range(e2e_steps):
+        e2e_step(parts[k])
     e1.record(stream)
     torch.cuda.synchronize()
+    e2e_clk = e2e_clocks.stop()
     e2e_ms = e0.elapsed_time(e1)
+    e2e_parts = {name: statistics.median(parts[k][j].elapsed_time(parts[k][j + 1]) for k in range(e2e_steps))
+                 for j, name in enumerate(("copy_in_ms", "update_ms", "copy_out_ms"))}
     if dist:
         t = torch.tensor([e2e_ms], device="cuda")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         e2e_ms = float(t.item())
-    io_bytes = n_end * (8 + 8 + 4)
+    del st2
+    io_bytes = n * (8 + 8 + 4)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -635,9 +659,11 @@ def main():
             "pairs_per_s": pairs / p2p_s,
             "mufu_bound_pairs_per_s": SMS * MUFU_LANES * sm_mhz * 1e6 / 2,
         },
-        "e2e": {"value": n_end * e2e_steps * world / (e2e_ms / 1e3), "unit": "particle-steps/s",
+        "e2e": {"value": n * e2e_steps * world / (e2e_ms / 1e3), "unit": "particle-steps/s",
+                "median_parts": e2e_parts, "clocks": e2e_clk,
                 "h2d_bytes_per_step": io_bytes, "d2h_bytes_per_step": io_bytes,
-                "api": "Stars.update(1) per step, state copied in from and out to pinned host memory"},
+                "api": "Stars.update(1) per step, state copied in from and out to pinned host memory; the same "
+                       "warm-up and timed steps as the device-timed value, from the same initial state"},
         "cpu_baseline": cpu,
         "gpu_launches": stars.kernel_launches(args.steps),
         "clocks": clk,

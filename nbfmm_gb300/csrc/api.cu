@@ -234,10 +234,7 @@ struct nbfmm_stars {
   float4* state4 = nullptr;
   float2* state_prev = nullptr;
   float2* sprev = nullptr;
-  float2* grave_cur = nullptr;
-  float2* grave_prev = nullptr;
-  float* w_by_orig = nullptr;
-  int* fate = nullptr;
+  float4* grave = nullptr;  // final states by original index: two float4 per star (stars.cuh file_grave)
   int* counters = nullptr;
   StepCounters sc{};
   cudaStream_t capture_stream = nullptr;
@@ -261,10 +258,7 @@ struct nbfmm_stars {
     NBFMM_TRY(dalloc(&state4, n, "state"));
     NBFMM_TRY(dalloc(&state_prev, n, "state prev"));
     NBFMM_TRY(dalloc(&sprev, n, "sorted prev"));
-    NBFMM_TRY(dalloc(&grave_cur, n, "final positions"));
-    NBFMM_TRY(dalloc(&grave_prev, n, "final previous positions"));
-    NBFMM_TRY(dalloc(&w_by_orig, n, "weights by index"));
-    NBFMM_TRY(dalloc(&fate, n, "fates"));
+    NBFMM_TRY(dalloc(&grave, 2 * n, "final states"));
     NBFMM_TRY(dalloc(&counters, 8, "step counters"));
     cudaMemset(cur, 0, n * sizeof(float2));
     cudaMemset(prev, 0, n * sizeof(float2));
@@ -307,7 +301,7 @@ struct nbfmm_stars {
     if (cap_b) cudaEventDestroy(cap_b);
     if (capture_stream) cudaStreamDestroy(capture_stream);
     dfree(cur); dfree(prev); dfree(w); dfree(state4); dfree(state_prev); dfree(sprev);
-    dfree(grave_cur); dfree(grave_prev); dfree(w_by_orig); dfree(fate); dfree(counters);
+    dfree(grave); dfree(counters);
     delete solver;
   }
 
@@ -316,8 +310,7 @@ struct nbfmm_stars {
   void enqueue_step(cudaStream_t s) {
     nbfmm_solver& v = *solver;
     const uint32_t dead = (uint32_t)v.num_cells;
-    launch_keys_from_state(v.geo, sc, state4, state_prev, dead, v.keys_a, v.vals_a, grave_cur, grave_prev, fate,
-                           max_n, s);
+    launch_keys_from_state(v.geo, sc, state4, state_prev, dead, v.keys_a, v.vals_a, grave, max_n, s);
     v.sort(sc.n_cur, v.key_bits, s);
     launch_head(v.skey, sc.n_cur, v.num_cells, v.head, sc.n_alive, s);
     launch_worklist(v.head, v.num_cells, v.work, v.d_work_count(), s);
@@ -386,7 +379,7 @@ struct nbfmm_stars {
     if (steps <= 0) return NBFMM_OK;
     if (!step_graph) NBFMM_TRY(build_graph());
     nbfmm_solver& v = *solver;
-    launch_import(sc, cur, prev, w, state4, state_prev, w_by_orig, max_n, s);
+    launch_import(sc, cur, prev, w, state4, state_prev, max_n, s);
     launch_set_int(sc.num_steps, steps, s);
     for (int k = 0; k < steps; ++k) {
       if (prof_used < prof_max) {  // point the P2P event nodes at this step's pair
@@ -402,23 +395,23 @@ struct nbfmm_stars {
     }
     // Final prune and the reference's order: survivors (fate 0) in original order, then the pruned stars,
     // most recent first (fate 1, 2, ...), each group in original order.
-    launch_export_fate(v.geo, sc, state4, state_prev, grave_cur, grave_prev, fate, max_n, s);
-    launch_fate_keys(sc, fate, v.keys_a, v.vals_a, max_n, s);
+    launch_export_fate(v.geo, sc, state4, state_prev, grave, max_n, s);
+    launch_fate_keys(sc, grave, v.keys_a, v.vals_a, max_n, s);
     v.sort(sc.n_import, fate_bits(steps), s);
     launch_head(v.skey, sc.n_import, 1, v.head, sc.num_star, s);  // head[1] = number of fate-0 stars
-    launch_export_gather(sc, v.perm, grave_cur, grave_prev, w_by_orig, cur, prev, w, max_n, s);
+    launch_export_gather(sc, v.perm, grave, cur, prev, w, max_n, s);
     return cuda_check("nbfmm_stars_update");
   }
 
   // Stars::prune (prune.cu:28-62) on the public arrays: the one-bit stable sort of prune.cu:60, with the count
-  // of kept stars (prune.cu:61) left in the device counter. The final-state files serve as scratch: they are
-  // only live inside an update call.
+  // of kept stars (prune.cu:61) left in the device counter. The final-state records serve as scratch: they
+  // are only live inside an update call.
   void prune(cudaStream_t s) {
     nbfmm_solver& v = *solver;
-    launch_prune_keys(v.geo, sc, cur, prev, w, v.keys_a, v.vals_a, grave_cur, grave_prev, w_by_orig, max_n, s);
+    launch_prune_keys(v.geo, sc, cur, prev, w, v.keys_a, v.vals_a, grave, max_n, s);
     v.sort(sc.n_import, 1, s);
     launch_head(v.skey, sc.n_import, 1, v.head, sc.num_star, s);  // head[1] = number of kept stars
-    launch_export_gather(sc, v.perm, grave_cur, grave_prev, w_by_orig, cur, prev, w, max_n, s);
+    launch_export_gather(sc, v.perm, grave, cur, prev, w, max_n, s);
   }
 
   // Stars::display (display.cu:219-229): the frame of the current stars, then prune.

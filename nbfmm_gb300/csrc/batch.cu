@@ -83,22 +83,18 @@ __global__ void batch_import_kernel(BatchDevice bd, StepCounters sc, const int* 
                                     const int* __restrict__ live_base, const float2* __restrict__ cur,
                                     const float2* __restrict__ prev, const float* __restrict__ w,
                                     float4* __restrict__ state4, float2* __restrict__ state_prev,
-                                    float* __restrict__ w_by_orig, float2* __restrict__ grave_cur,
-                                    float2* __restrict__ grave_prev, int* __restrict__ fate, int n, int old_fate) {
+                                    float4* __restrict__ grave, int n, int old_fate) {
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     const int s = bd.sys_of_orig[i];
     const int local = i - bd.part_off[s];
     const float2 c = cur[i];
     const float m = w[i];
-    w_by_orig[i] = m;
     if (local < counts[s]) {
       const int slot = live_base[s] + local;
       state4[slot] = make_float4(c.x, c.y, m, __int_as_float(i));
       state_prev[slot] = prev[i];
     } else {
-      grave_cur[i] = c;
-      grave_prev[i] = prev[i];
-      fate[i] = old_fate;
+      file_grave(grave, i, c.x, c.y, prev[i], m, old_fate);
     }
   }
   if (blockIdx.x == 0 && threadIdx.x == 0) {
@@ -112,8 +108,7 @@ __global__ void batch_import_kernel(BatchDevice bd, StepCounters sc, const int* 
 __global__ void batch_keys_kernel(BatchDevice bd, StepCounters sc, const float4* __restrict__ state4,
                                   const float2* __restrict__ state_prev, uint32_t dead_key,
                                   uint32_t* __restrict__ keys, uint32_t* __restrict__ vals,
-                                  float2* __restrict__ grave_cur, float2* __restrict__ grave_prev,
-                                  int* __restrict__ fate) {
+                                  float4* __restrict__ grave) {
   const int n = *sc.n_cur;
   const int prune = *sc.prune;
   const int death_rank = *sc.num_steps + 1 - (*sc.step - 1);
@@ -125,9 +120,7 @@ __global__ void batch_keys_kernel(BatchDevice bd, StepCounters sc, const float4*
     uint32_t key;
     if (prune && outside(g, p.x, p.y)) {  // prune.cu:40-41 with the system's limits
       key = dead_key;
-      grave_cur[orig] = make_float2(p.x, p.y);
-      grave_prev[orig] = state_prev[i];
-      fate[orig] = death_rank;
+      file_grave(grave, orig, p.x, p.y, state_prev[i], p.z, death_rank);
     } else {
       key = (uint32_t)bd.cell_base[s] + leaf_key(g, p.x, p.y);
     }
@@ -184,26 +177,23 @@ batch_m2l_kernel(const float4* __restrict__ cell4, float2* __restrict__ ceff, co
 
 // Final prune of the call, and every star's final state filed by original index (fate 0 = alive).
 __global__ void batch_export_fate_kernel(BatchDevice bd, StepCounters sc, const float4* __restrict__ state4,
-                                         const float2* __restrict__ state_prev, float2* __restrict__ grave_cur,
-                                         float2* __restrict__ grave_prev, int* __restrict__ fate) {
+                                         const float2* __restrict__ state_prev, float4* __restrict__ grave) {
   const int n = *sc.n_cur;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     const float4 p = state4[i];
     const int orig = __float_as_int(p.w);
-    grave_cur[orig] = make_float2(p.x, p.y);
-    grave_prev[orig] = state_prev[i];
-    fate[orig] = outside(bd.geo[bd.sys_of_orig[orig]], p.x, p.y) ? 1 : 0;
+    file_grave(grave, orig, p.x, p.y, state_prev[i], p.z, outside(bd.geo[bd.sys_of_orig[orig]], p.x, p.y) ? 1 : 0);
   }
 }
 
 // Export keys: system-major, then fate, so each system's block keeps survivors first, then the pruned stars,
 // most recently pruned first -- the order num_steps reference updates leave that system's arrays in.
-__global__ void batch_fate_keys_kernel(BatchDevice bd, StepCounters sc, const int* __restrict__ fate,
+__global__ void batch_fate_keys_kernel(BatchDevice bd, StepCounters sc, const float4* __restrict__ grave,
                                        uint32_t* __restrict__ keys, uint32_t* __restrict__ vals) {
   const int n = *sc.n_import;
   const int span = *sc.num_steps + 2;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-    keys[i] = (uint32_t)(bd.sys_of_orig[i] * span + fate[i]);
+    keys[i] = (uint32_t)(bd.sys_of_orig[i] * span + grave_fate(grave, i));
     vals[i] = (uint32_t)i;
   }
 }
@@ -310,9 +300,7 @@ struct nbfmm_batch {
   float* w = nullptr;
   float4* state4 = nullptr;
   float2* state_prev = nullptr;
-  float2 *grave_cur = nullptr, *grave_prev = nullptr;
-  float* w_by_orig = nullptr;
-  int* fate = nullptr;
+  float4* grave = nullptr;  // final states by original index: two float4 per star (stars.cuh file_grave)
   int* sys_counts = nullptr;  // survivors per system
   int* live_base = nullptr;   // [S + 1] prefix of sys_counts
   int* part_off = nullptr;    // [S + 1] particle ranges
@@ -421,10 +409,7 @@ struct nbfmm_batch {
     BATCH_TRY(balloc(&w, N, "weight"));
     BATCH_TRY(balloc(&state4, N, "state"));
     BATCH_TRY(balloc(&state_prev, N, "state prev"));
-    BATCH_TRY(balloc(&grave_cur, N, "final positions"));
-    BATCH_TRY(balloc(&grave_prev, N, "final previous positions"));
-    BATCH_TRY(balloc(&w_by_orig, N, "weights by index"));
-    BATCH_TRY(balloc(&fate, N, "fates"));
+    BATCH_TRY(balloc(&grave, 2 * (size_t)N, "final states"));
     BATCH_TRY(balloc(&sys_counts, (size_t)S, "system counts"));
     BATCH_TRY(balloc(&live_base, (size_t)S + 1, "live prefix"));
     BATCH_TRY(balloc(&part_off, (size_t)S + 1, "particle offsets"));
@@ -471,8 +456,8 @@ struct nbfmm_batch {
     bfree(geo); bfree(sys_of_orig); bfree(cell_base); bfree(dim); bfree(levels); bfree(level_base); bfree(tile_base);
     bfree(keys_a); bfree(vals_a); bfree(keys_b); bfree(vals_b); bfree(counts); bfree(digit_total);
     bfree(head); bfree(work); bfree(sorted4); bfree(sprev); bfree(cell4); bfree(ceff);
-    bfree(cur); bfree(prev); bfree(w); bfree(state4); bfree(state_prev); bfree(grave_cur); bfree(grave_prev);
-    bfree(w_by_orig); bfree(fate); bfree(sys_counts); bfree(live_base); bfree(part_off); bfree(ints);
+    bfree(cur); bfree(prev); bfree(w); bfree(state4); bfree(state_prev); bfree(grave); bfree(sys_counts);
+    bfree(live_base); bfree(part_off); bfree(ints);
   }
 
   int alloc_head() {
@@ -503,8 +488,7 @@ struct nbfmm_batch {
   void enqueue_step(cudaStream_t s) {
     const int N = std::max(n, 1);
     batch_keys_kernel<<<grid_for(N, 256, 152 * 16), 256, 0, s>>>(device(), sc, state4, state_prev,
-                                                                (uint32_t)total_leaf, keys_a, vals_a, grave_cur,
-                                                                grave_prev, fate);
+                                                                (uint32_t)total_leaf, keys_a, vals_a, grave);
     sort(sc.n_cur, key_bits, s);
     launch_head(skey, sc.n_cur, total_leaf, head, sc.n_alive, s);
     launch_worklist(head, total_leaf, work, d_work_count(), s);
@@ -593,8 +577,7 @@ struct nbfmm_batch {
     const int N = std::max(n, 1);
     batch_live_scan_kernel<<<1, 1024, 0, s>>>(sys_counts, S, live_base);
     batch_import_kernel<<<grid_for(N, 256, 152 * 16), 256, 0, s>>>(device(), sc, sys_counts, live_base, cur, prev, w,
-                                                                   state4, state_prev, w_by_orig, grave_cur,
-                                                                   grave_prev, fate, n, steps + 1);
+                                                                   state4, state_prev, grave, n, steps + 1);
     launch_set_int(sc.num_steps, steps, s);
     for (int k = 0; k < steps; ++k) {
       if (prof_used < prof_max) {
@@ -608,12 +591,11 @@ struct nbfmm_batch {
       }
       if (cudaGraphLaunch(graph, s) != cudaSuccess) return cuda_status("cudaGraphLaunch");
     }
-    batch_export_fate_kernel<<<grid_for(N, 256, 152 * 16), 256, 0, s>>>(device(), sc, state4, state_prev, grave_cur,
-                                                                       grave_prev, fate);
-    batch_fate_keys_kernel<<<grid_for(N, 256, 152 * 16), 256, 0, s>>>(device(), sc, fate, keys_a, vals_a);
+    batch_export_fate_kernel<<<grid_for(N, 256, 152 * 16), 256, 0, s>>>(device(), sc, state4, state_prev, grave);
+    batch_fate_keys_kernel<<<grid_for(N, 256, 152 * 16), 256, 0, s>>>(device(), sc, grave, keys_a, vals_a);
     sort(sc.n_import, fate_bits(S, steps), s);
     batch_counts_kernel<<<grid_for(S, 256, 152), 256, 0, s>>>(skey, sc, S, sys_counts);
-    launch_export_gather(sc, perm, grave_cur, grave_prev, w_by_orig, cur, prev, w, N, s);
+    launch_export_gather(sc, perm, grave, cur, prev, w, N, s);
     return cuda_status("nbfmm_batch_update");
   }
 };

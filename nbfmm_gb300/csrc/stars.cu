@@ -21,14 +21,12 @@ namespace {
 
 __global__ void import_kernel(StepCounters sc, const float2* __restrict__ cur, const float2* __restrict__ prev,
                               const float* __restrict__ w, float4* __restrict__ state4,
-                              float2* __restrict__ state_prev, float* __restrict__ w_by_orig) {
+                              float2* __restrict__ state_prev) {
   const int n = *sc.num_star;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     const float2 c = cur[i];
-    const float m = w[i];
-    state4[i] = make_float4(c.x, c.y, m, __int_as_float(i));
+    state4[i] = make_float4(c.x, c.y, w[i], __int_as_float(i));
     state_prev[i] = prev[i];
-    w_by_orig[i] = m;
   }
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     *sc.n_cur = n;
@@ -41,8 +39,7 @@ __global__ void import_kernel(StepCounters sc, const float2* __restrict__ cur, c
 __global__ void keys_from_state_kernel(Geometry g, StepCounters sc, const float4* __restrict__ state4,
                                        const float2* __restrict__ state_prev, uint32_t dead_key,
                                        uint32_t* __restrict__ keys, uint32_t* __restrict__ vals,
-                                       float2* __restrict__ grave_cur, float2* __restrict__ grave_prev,
-                                       int* __restrict__ fate) {
+                                       float4* __restrict__ grave) {
   const int n = *sc.n_cur;
   const int prune = *sc.prune;
   const int death_rank = *sc.num_steps + 1 - (*sc.step - 1);  // later deaths first in the final order
@@ -51,10 +48,7 @@ __global__ void keys_from_state_kernel(Geometry g, StepCounters sc, const float4
     uint32_t key;
     if (prune && outside(g, p.x, p.y)) {
       key = dead_key;
-      const int orig = __float_as_int(p.w);
-      grave_cur[orig] = make_float2(p.x, p.y);
-      grave_prev[orig] = state_prev[i];
-      fate[orig] = death_rank;
+      file_grave(grave, __float_as_int(p.w), p.x, p.y, state_prev[i], p.z, death_rank);
     } else {
       key = leaf_key(g, p.x, p.y);
     }
@@ -96,37 +90,33 @@ __global__ void finish_step_kernel(StepCounters sc) {
 // The last prune of the call (prune.cu:40-41 on the final positions), and every star's final state filed by
 // original index: fate 0 = alive, fate 1 = pruned by the last step.
 __global__ void export_fate_kernel(Geometry g, StepCounters sc, const float4* __restrict__ state4,
-                                   const float2* __restrict__ state_prev, float2* __restrict__ grave_cur,
-                                   float2* __restrict__ grave_prev, int* __restrict__ fate) {
+                                   const float2* __restrict__ state_prev, float4* __restrict__ grave) {
   const int n = *sc.n_cur;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     const float4 p = state4[i];
-    const int orig = __float_as_int(p.w);
-    grave_cur[orig] = make_float2(p.x, p.y);
-    grave_prev[orig] = state_prev[i];
-    fate[orig] = outside(g, p.x, p.y) ? 1 : 0;
+    file_grave(grave, __float_as_int(p.w), p.x, p.y, state_prev[i], p.z, outside(g, p.x, p.y) ? 1 : 0);
   }
 }
 
-__global__ void fate_keys_kernel(StepCounters sc, const int* __restrict__ fate, uint32_t* __restrict__ keys,
+__global__ void fate_keys_kernel(StepCounters sc, const float4* __restrict__ grave, uint32_t* __restrict__ keys,
                                  uint32_t* __restrict__ vals) {
   const int n = *sc.n_import;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-    keys[i] = (uint32_t)fate[i];
+    keys[i] = (uint32_t)grave_fate(grave, i);
     vals[i] = (uint32_t)i;
   }
 }
 
 __global__ void export_gather_kernel(StepCounters sc, const uint32_t* __restrict__ order,
-                                     const float2* __restrict__ grave_cur, const float2* __restrict__ grave_prev,
-                                     const float* __restrict__ w_by_orig, float2* __restrict__ cur,
+                                     const float4* __restrict__ grave, float2* __restrict__ cur,
                                      float2* __restrict__ prev, float* __restrict__ w) {
   const int n = *sc.n_import;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     const uint32_t o = order[i];
-    cur[i] = grave_cur[o];
-    prev[i] = grave_prev[o];
-    w[i] = w_by_orig[o];
+    const float4 a = grave[2 * o];
+    cur[i] = make_float2(a.x, a.y);
+    prev[i] = make_float2(a.z, a.w);
+    w[i] = grave[2 * o + 1].x;
   }
 }
 
@@ -135,16 +125,14 @@ __global__ void set_int_kernel(int* p, int v) { *p = v; }
 __global__ void prune_keys_kernel(Geometry g, StepCounters sc, const float2* __restrict__ cur,
                                   const float2* __restrict__ prev, const float* __restrict__ w,
                                   uint32_t* __restrict__ keys, uint32_t* __restrict__ vals,
-                                  float2* __restrict__ tmp_cur, float2* __restrict__ tmp_prev,
-                                  float* __restrict__ tmp_w) {
+                                  float4* __restrict__ grave) {
   const int n = *sc.num_star;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     const float2 c = cur[i];
-    keys[i] = outside(g, c.x, c.y) ? 1u : 0u;  // prune.cu:40-41
+    const int out = outside(g, c.x, c.y) ? 1 : 0;  // prune.cu:40-41
+    keys[i] = (uint32_t)out;
     vals[i] = (uint32_t)i;
-    tmp_cur[i] = c;
-    tmp_prev[i] = prev[i];
-    tmp_w[i] = w[i];
+    file_grave(grave, i, c.x, c.y, prev[i], w[i], out);
   }
   if (blockIdx.x == 0 && threadIdx.x == 0) *sc.n_import = n;
 }
@@ -161,15 +149,15 @@ int grid_for(long long n, int threads, int cap) {
 void launch_set_int(int* p, int v, cudaStream_t stream) { set_int_kernel<<<1, 1, 0, stream>>>(p, v); }
 
 void launch_import(const StepCounters& sc, const float2* cur, const float2* prev, const float* w, float4* state4,
-                   float2* state_prev, float* w_by_orig, int max_n, cudaStream_t stream) {
-  import_kernel<<<grid_for(max_n, 256, 152 * 16), 256, 0, stream>>>(sc, cur, prev, w, state4, state_prev, w_by_orig);
+                   float2* state_prev, int max_n, cudaStream_t stream) {
+  import_kernel<<<grid_for(max_n, 256, 152 * 16), 256, 0, stream>>>(sc, cur, prev, w, state4, state_prev);
 }
 
 void launch_keys_from_state(const Geometry& g, const StepCounters& sc, const float4* state4, const float2* state_prev,
-                            uint32_t dead_key, uint32_t* keys, uint32_t* vals, float2* grave_cur, float2* grave_prev,
-                            int* fate, int max_n, cudaStream_t stream) {
+                            uint32_t dead_key, uint32_t* keys, uint32_t* vals, float4* grave, int max_n,
+                            cudaStream_t stream) {
   keys_from_state_kernel<<<grid_for(max_n, 256, 152 * 16), 256, 0, stream>>>(g, sc, state4, state_prev, dead_key, keys,
-                                                                             vals, grave_cur, grave_prev, fate);
+                                                                             vals, grave);
 }
 
 void launch_gather_state_p2m(const Geometry& g, const int* head, const uint32_t* perm, const float4* state4,
@@ -190,28 +178,23 @@ void launch_gather_state_p2m_cells(const int* head, int num_cells, const uint32_
 void launch_finish_step(const StepCounters& sc, cudaStream_t stream) { finish_step_kernel<<<1, 1, 0, stream>>>(sc); }
 
 void launch_export_fate(const Geometry& g, const StepCounters& sc, const float4* state4, const float2* state_prev,
-                        float2* grave_cur, float2* grave_prev, int* fate, int max_n, cudaStream_t stream) {
-  export_fate_kernel<<<grid_for(max_n, 256, 152 * 16), 256, 0, stream>>>(g, sc, state4, state_prev, grave_cur,
-                                                                         grave_prev, fate);
+                        float4* grave, int max_n, cudaStream_t stream) {
+  export_fate_kernel<<<grid_for(max_n, 256, 152 * 16), 256, 0, stream>>>(g, sc, state4, state_prev, grave);
 }
 
-void launch_fate_keys(const StepCounters& sc, const int* fate, uint32_t* keys, uint32_t* vals, int max_n,
+void launch_fate_keys(const StepCounters& sc, const float4* grave, uint32_t* keys, uint32_t* vals, int max_n,
                       cudaStream_t stream) {
-  fate_keys_kernel<<<grid_for(max_n, 256, 152 * 16), 256, 0, stream>>>(sc, fate, keys, vals);
+  fate_keys_kernel<<<grid_for(max_n, 256, 152 * 16), 256, 0, stream>>>(sc, grave, keys, vals);
 }
 
-void launch_export_gather(const StepCounters& sc, const uint32_t* order, const float2* grave_cur,
-                          const float2* grave_prev, const float* w_by_orig, float2* cur, float2* prev, float* w,
-                          int max_n, cudaStream_t stream) {
-  export_gather_kernel<<<grid_for(max_n, 256, 152 * 16), 256, 0, stream>>>(sc, order, grave_cur, grave_prev, w_by_orig,
-                                                                           cur, prev, w);
+void launch_export_gather(const StepCounters& sc, const uint32_t* order, const float4* grave, float2* cur,
+                          float2* prev, float* w, int max_n, cudaStream_t stream) {
+  export_gather_kernel<<<grid_for(max_n, 256, 152 * 16), 256, 0, stream>>>(sc, order, grave, cur, prev, w);
 }
 
 void launch_prune_keys(const Geometry& g, const StepCounters& sc, const float2* cur, const float2* prev,
-                       const float* w, uint32_t* keys, uint32_t* vals, float2* tmp_cur, float2* tmp_prev,
-                       float* tmp_w, int max_n, cudaStream_t stream) {
-  prune_keys_kernel<<<grid_for(max_n, 256, 152 * 16), 256, 0, stream>>>(g, sc, cur, prev, w, keys, vals, tmp_cur,
-                                                                        tmp_prev, tmp_w);
+                       const float* w, uint32_t* keys, uint32_t* vals, float4* grave, int max_n, cudaStream_t stream) {
+  prune_keys_kernel<<<grid_for(max_n, 256, 152 * 16), 256, 0, stream>>>(g, sc, cur, prev, w, keys, vals, grave);
 }
 
 }  // namespace nbfmm_gb300

@@ -16,12 +16,26 @@ struct StepCounters {
   int* num_steps;  // steps of the current call
 };
 
+// The final state of a star filed under its original index ("grave"): a 32-byte record of two float4,
+// (x, y, x_prev, y_prev) and (m, fate as int bits, 0, 0), at grave[2 * orig] and grave[2 * orig + 1]. One thread
+// writes both halves, so a record scattered by original index fills one DRAM sector instead of three partial
+// ones. Fate 0 = alive at the end of the call; k > 0 orders the pruned stars (smaller = pruned later).
+__device__ __forceinline__ void file_grave(float4* __restrict__ grave, int orig, float x, float y, float2 prev, float m,
+                                           int fate) {
+  grave[2 * orig] = make_float4(x, y, prev.x, prev.y);
+  grave[2 * orig + 1] = make_float4(m, __int_as_float(fate), 0.0f, 0.0f);
+}
+
+__device__ __forceinline__ int grave_fate(const float4* __restrict__ grave, int orig) {
+  return __float_as_int(grave[2 * orig + 1].y);
+}
+
 void launch_set_int(int* p, int v, cudaStream_t stream);
 void launch_import(const StepCounters& sc, const float2* cur, const float2* prev, const float* w, float4* state4,
-                   float2* state_prev, float* w_by_orig, int max_n, cudaStream_t stream);
+                   float2* state_prev, int max_n, cudaStream_t stream);
 void launch_keys_from_state(const Geometry& g, const StepCounters& sc, const float4* state4, const float2* state_prev,
-                            uint32_t dead_key, uint32_t* keys, uint32_t* vals, float2* grave_cur, float2* grave_prev,
-                            int* fate, int max_n, cudaStream_t stream);
+                            uint32_t dead_key, uint32_t* keys, uint32_t* vals, float4* grave, int max_n,
+                            cudaStream_t stream);
 void launch_gather_state_p2m(const Geometry& g, const int* head, const uint32_t* perm, const float4* state4,
                              const float2* state_prev, float4* sorted4, float2* sprev, float4* cell0,
                              cudaStream_t stream);
@@ -31,18 +45,16 @@ void launch_gather_state_p2m_cells(const int* head, int num_cells, const uint32_
                                    cudaStream_t stream);
 void launch_finish_step(const StepCounters& sc, cudaStream_t stream);
 void launch_export_fate(const Geometry& g, const StepCounters& sc, const float4* state4, const float2* state_prev,
-                        float2* grave_cur, float2* grave_prev, int* fate, int max_n, cudaStream_t stream);
-void launch_fate_keys(const StepCounters& sc, const int* fate, uint32_t* keys, uint32_t* vals, int max_n,
+                        float4* grave, int max_n, cudaStream_t stream);
+void launch_fate_keys(const StepCounters& sc, const float4* grave, uint32_t* keys, uint32_t* vals, int max_n,
                       cudaStream_t stream);
-void launch_export_gather(const StepCounters& sc, const uint32_t* order, const float2* grave_cur,
-                          const float2* grave_prev, const float* w_by_orig, float2* cur, float2* prev, float* w,
-                          int max_n, cudaStream_t stream);
+void launch_export_gather(const StepCounters& sc, const uint32_t* order, const float4* grave, float2* cur,
+                          float2* prev, float* w, int max_n, cudaStream_t stream);
 
 // Stars::prune on the public arrays (prune.cu:28-62), step 1: n_import = num_star, keys 1 for the stars outside
-// the limits and 0 otherwise, vals the identity, and a copy of the arrays into tmp_* to gather back from.
+// the limits and 0 otherwise, vals the identity, and a copy of the arrays into grave records to gather back from.
 void launch_prune_keys(const Geometry& g, const StepCounters& sc, const float2* cur, const float2* prev,
-                       const float* w, uint32_t* keys, uint32_t* vals, float2* tmp_cur, float2* tmp_prev,
-                       float* tmp_w, int max_n, cudaStream_t stream);
+                       const float* w, uint32_t* keys, uint32_t* vals, float4* grave, int max_n, cudaStream_t stream);
 
 // Frame raster of Stars::display (display.cu): clears the frame and draws stars [0, n) where n = *d_n, or n_host
 // when d_n is null (grid sized for max_n).
