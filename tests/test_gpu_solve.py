@@ -53,6 +53,28 @@ def test_uniform_sizes(engine, orc, n, level):
     assert_solve_parity(eff, pos, w, level, lim, 1e-3, orc)
 
 
+@pytest.mark.parametrize("scale,eps,level", [
+    (1.0, 1e-3, 4),
+    (200.0, 5.0, 4),    # a strongly cancelling far field
+    (600.0, 50.0, 4),   # large coordinates
+    (1.0, 1e-12, 3),    # tiny softening: r^3 + eps spans many binades
+    (1.0, 5e9, 3),      # softening far above r^3
+])
+def test_scaled_fields_and_extreme_softening(engine, orc, scale, eps, level):
+    """The near field's reciprocal arithmetic (hardware approximation and the FMA-pipe iteration) over coordinate
+    scales and softenings far from the benchmark's, against the oracle."""
+    rng = np.random.default_rng(int(scale * 7 + level))
+    n = 20000
+    r = np.sqrt(rng.uniform(0, 1, n))
+    a = rng.uniform(0, 2 * np.pi, n)
+    pos = (scale * np.stack([r * np.cos(a), r * np.sin(a)], 1)).astype(np.float32)
+    w = rng.uniform(0.5, 1.5, n).astype(np.float32)
+    lim = (-1.01 * scale, -1.01 * scale, 1.01 * scale, 1.01 * scale)
+    s, eff = run_solve(engine, pos, w, level, lim, eps)
+    assert np.all(np.isfinite(eff))
+    assert_solve_parity(eff, pos, w, level, lim, eps, orc)
+
+
 def test_disk_against_oracle_and_fp64(engine, orc):
     from nbfmm_gb300 import workloads
 
