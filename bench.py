@@ -477,9 +477,9 @@ def main():
     if args.config == "display_16m" and args.impl == "gb300":
         return run_display(args)
 
-    rank = int(os.environ.get("RANK", "0"))
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
+    from nbfmm_gb300 import replicas
+
+    rank, world, local = replicas.rank_info()
     if args.impl == "reference" and args.config not in workloads.CONFIGS:
         if rank == 0:
             run_reference_mode(args)
@@ -495,11 +495,7 @@ def main():
     import nbfmm_gb300
 
     torch.cuda.set_device(local)
-    dist = None
-    if world > 1:
-        import torch.distributed as dist
-
-        dist.init_process_group("nccl")
+    dist = replicas.init(world, "nccl")
     dev_id = str(local)
     try:
         dev_id = "GPU-" + str(torch.cuda.get_device_properties(local).uuid)
@@ -535,8 +531,7 @@ def main():
 
     # ---- timed region: K steps in one update call, P2P timed per launch with CUDA events ----
     stars.profile_begin(args.steps)
-    if dist:
-        dist.barrier()
+    replicas.barrier(dist)
     torch.cuda.synchronize()
     clocks = ClockSampler(dev_id)
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -544,13 +539,10 @@ def main():
     stars.update(args.steps)
     ev1.record(stream)
     torch.cuda.synchronize()
+    replicas.barrier(dist)
     clk = clocks.stop()
-    elapsed_ms = ev0.elapsed_time(ev1)
+    elapsed_ms = replicas.max_over_ranks(ev0.elapsed_time(ev1), dist, "cuda")
     p2p_ms, p2p_launches = stars.profile_end()
-    if dist:
-        t = torch.tensor([elapsed_ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        elapsed_ms = float(t.item())
     n_end = stars.num_star_
 
     # Pair count at the end of the timed steps (the system moves); the roofline uses the mean of both ends.
@@ -593,8 +585,7 @@ def main():
     for _ in range(args.warmup):
         e2e_step()
     torch.cuda.synchronize()
-    if dist:
-        dist.barrier()
+    replicas.barrier(dist)
     parts = [[torch.cuda.Event(enable_timing=True) for _ in range(4)] for _ in range(e2e_steps)]
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e2e_clocks = ClockSampler(dev_id)
@@ -603,14 +594,11 @@ def main():
         e2e_step(parts[k])
     e1.record(stream)
     torch.cuda.synchronize()
+    replicas.barrier(dist)
     e2e_clk = e2e_clocks.stop()
-    e2e_ms = e0.elapsed_time(e1)
+    e2e_ms = replicas.max_over_ranks(e0.elapsed_time(e1), dist, "cuda")
     e2e_parts = {name: statistics.median(parts[k][j].elapsed_time(parts[k][j + 1]) for k in range(e2e_steps))
                  for j, name in enumerate(("copy_in_ms", "update_ms", "copy_out_ms"))}
-    if dist:
-        t = torch.tensor([e2e_ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_ms = float(t.item())
     del st2
     io_bytes = n * (8 + 8 + 4)
 
@@ -623,7 +611,7 @@ def main():
 
     if rank != 0:
         return
-    value = n * args.steps * world / (elapsed_ms / 1e3)
+    value = replicas.whole_job_rate(n * args.steps, world, elapsed_ms)
     p2p_s = p2p_ms / max(p2p_launches, 1) / 1e3
     sm_mhz = clk["sm_mhz"] or measured_sm_mhz()
     fp32_peak = SMS * FP32_LANES * 2 * sm_mhz * 1e6 / 1e12
@@ -659,7 +647,7 @@ def main():
             "pairs_per_s": pairs / p2p_s,
             "mufu_bound_pairs_per_s": SMS * MUFU_LANES * sm_mhz * 1e6 / 2,
         },
-        "e2e": {"value": n * e2e_steps * world / (e2e_ms / 1e3), "unit": "particle-steps/s",
+        "e2e": {"value": replicas.whole_job_rate(n * e2e_steps, world, e2e_ms), "unit": "particle-steps/s",
                 "median_parts": e2e_parts, "clocks": e2e_clk,
                 "h2d_bytes_per_step": io_bytes, "d2h_bytes_per_step": io_bytes,
                 "api": "Stars.update(1) per step, state copied in from and out to pinned host memory; the same "
@@ -670,8 +658,7 @@ def main():
         "error_vs_fp64": err64,
     }
     print(json.dumps(out), flush=True)
-    if dist:
-        dist.destroy_process_group()
+    replicas.finish(dist)
 
 
 if __name__ == "__main__":
