@@ -107,7 +107,9 @@ def run_reference_arm(args, sysm, rank):
     tick = sysm.tick()
     n = n0
     for _ in range(args.warmup):
-        n, cur[:n], prev[:n], w[:n], _ = oracle.stars_update(cur[:n], prev[:n], w[:n], level, lim, sysm.epsilon, tick)
+        # the new count is bound last: the slices on the left take the count the step started with
+        k, cur[:n], prev[:n], w[:n], _ = oracle.stars_update(cur[:n], prev[:n], w[:n], level, lim, sysm.epsilon, tick)
+        n = k
     done, t0 = 0, time.perf_counter()
     for _ in range(args.steps):
         k, cur[:n], prev[:n], w[:n], _ = oracle.stars_update(cur[:n], prev[:n], w[:n], level, lim, sysm.epsilon, tick)

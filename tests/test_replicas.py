@@ -34,7 +34,8 @@ def replica_state(steps=3):
     w = np.full(n, 1.0 / n, np.float32)
     lim = (-1.5, -1.5, 1.5, 1.5)
     for _ in range(steps):
-        n, cur[:n], prev[:n], w[:n], _ = O.stars_update(cur[:n], prev[:n], w[:n], 3, lim, 1e-3, 1e-3)
+        k, cur[:n], prev[:n], w[:n], _ = O.stars_update(cur[:n], prev[:n], w[:n], 3, lim, 1e-3, 1e-3)
+        n = k
     return cur, prev, w, n
 
 
