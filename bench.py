@@ -135,7 +135,11 @@ def run_reference_mode(args):
     and the adjoint have no counterpart in the reference."""
     if args.config != "display_16m":
         why = {"batched_512": "the reference has no batched form (it steps one system per Stars)",
-               "adjoint_262k": "the reference has no adjoint"}.get(args.config, f"unknown config {args.config}")
+               "adjoint_262k": "the reference has no adjoint",
+               "models_16m": "the reference's models run only on a GPU (curand); the oracle restates their "
+                             "arithmetic for the gb300 line's cpu_baseline",
+               "movie_disk": "the reference's movie program runs only on a GPU; the gb300 line's cpu_baseline "
+                             "times the oracle's frame loop"}.get(args.config, f"unknown config {args.config}")
         print(json.dumps({"impl": "reference", "unavailable": why}), flush=True)
         return
     from nbfmm_gb300 import workloads
@@ -468,6 +472,151 @@ def run_display(args):
     print(json.dumps(out), flush=True)
 
 
+def run_models(args):
+    """The reference's initial-condition models (source/nbfmm/model): the centred double disk of the movie program
+    generated for 16.8M stars on the device (curand_init(0, idx, 0) per star, then the orbit arithmetic)."""
+    import torch
+
+    import nbfmm_gb300
+    from nbfmm_gb300 import model
+
+    n1, n2 = 10_485_760, 6_291_456  # 5:3, as the double-disk script
+    n = n1 + n2
+    cur = torch.empty(n, 2, device="cuda")
+    prev = torch.empty(n, 2, device="cuda")
+    w = torch.empty(n, device="cuda")
+    c1, c2, r1, r2, tick = (-0.5, 0.0), (0.5, 0.0), 0.3, 0.2, 5e-5
+
+    def gen():
+        model.generateDoubleDiskCenter(n1, n2, c1, c2, r1, r2, 1.0 / n, 10.0, 6.0, 1.0, tick, cur, prev, w)
+
+    for _ in range(max(3, args.warmup)):
+        gen()
+    torch.cuda.synchronize()
+    clocks = ClockSampler("0")
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(args.steps):
+        gen()
+    e1.record()
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    ms = e0.elapsed_time(e1) / args.steps
+    cpu = None
+    if not args.no_cpu_baseline:
+        from oracle import oracle
+
+        oracle.lib()
+        m = 1 << 20
+        u = np.random.default_rng(0).uniform(1e-7, 1.0, (m, 3)).astype(np.float32)
+        t0 = time.perf_counter()
+        oracle.model("double_disk_center", 0, u, n1=m * 5 // 8, n2=m * 3 // 8, center1=c1, center2=c2, radius1=r1,
+                     radius2=r2, weight=1.0 / n, center_weight1=10.0, center_weight2=6.0, eccentricity=1.0,
+                     tick=tick)
+        el = time.perf_counter() - t0
+        cpu = {"value": m / el, "unit": "stars/s", "cores": 1, "kind": "port",
+               "sample": f"{m:,} stars of the same model, the oracle's arithmetic on host-drawn uniforms "
+                         "(no CPU code reproduces curand's stream)"}
+    out = {
+        "metric": "stars/s", "value": n / (ms / 1e3), "unit": "stars/s", "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "generated (the model itself)",
+        "config": {"workload": f"generateDoubleDiskCenter: {n1:,} + {n2:,} stars, radii {r1}/{r2}, centre weights 10/6"},
+        "roofline": {"kernel": "disk_kernel (curand_init + orbit arithmetic) x2 + shift_kernel x2", "bound": "hbm",
+                     "unit": "GB/s", "achieved": 20 * n / (ms / 1e3) / 1e9,
+                     "peak": json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))["hbm_gbs"],
+                     "frac": 20 * n / (ms / 1e3) / 1e9 / json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))["hbm_gbs"],
+                     "traffic": None, "note": "20 B written per star; bound by curand_init's skip-ahead per star"},
+        "cpu_baseline": cpu, "gpu_launches": 4 * args.steps, "clocks": clk,
+        "e2e": {"value": n / (ms / 1e3), "unit": "stars/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0,
+                "api": "model.generateDoubleDiskCenter on device arrays (no host data)"},
+    }
+    print(json.dumps(out), flush=True)
+
+
+def run_movie(args):
+    """The movie program on the reference's disk script preset (main/script/disk.py: 10,000 stars, 1024 x 768,
+    60 fps, FMM level 4, a 16 x 12 domain at display scale 0.5). value = frames per second of the frame loop
+    (update, display, frame copy, file write) through the Python API, timed on the device; e2e = frames per second
+    of the nbfmm_main process itself, wall clock, start to exit."""
+    import tempfile
+
+    import torch
+
+    import nbfmm_gb300
+    from nbfmm_gb300 import build, launch, model
+
+    frames = max(60, args.steps)
+    argv = launch.preset("disk", num_second=1)
+    argv[2] = str(frames)  # fps = frames, 1 second: `frames` frames
+    width, height, fps, _, level, n, pw, ph, ds, g, ss = (float(a) for a in argv[:11])
+    width, height, fps, level, n = int(width), int(height), int(fps), int(level), int(n)
+    radius, weight = float(argv[12]), float(argv[13])
+    tick = float(np.float32(0.05 / fps))
+    plim = (-pw / 2, -ph / 2, pw / 2, ph / 2)
+    dlim = tuple(v * ds for v in plim)
+    with tempfile.TemporaryDirectory() as tmp:
+        st = nbfmm_gb300.Stars(level, n, width, height, fps, tick, g, ss, plim, dlim)
+        st.initialize(model.generateDisk, n, (0.0, 0.0), radius, weight)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with nbfmm_gb300.Movie(st, os.path.join(tmp, "api.y4m")) as mv:
+            mv.frame()
+            for _ in range(min(args.warmup, frames - 1)):
+                st.update(1)
+                mv.frame()
+            torch.cuda.synchronize()
+            e0.record()
+            for _ in range(frames):
+                st.update(1)
+                mv.frame()
+            e1.record()
+            mv.close()
+        torch.cuda.synchronize()
+        api_ms = e0.elapsed_time(e1)
+        exe = build.program("nbfmm_main")
+        if not os.path.exists(exe):
+            build.build()
+        w0 = time.perf_counter()
+        r = subprocess.run([exe, os.path.join(tmp, "cli.y4m")] + argv, capture_output=True)
+        cli_s = time.perf_counter() - w0
+        assert r.returncode == 0, r.stderr[-500:]
+    cpu = None
+    if not args.no_cpu_baseline:
+        from oracle import oracle
+
+        oracle.lib()
+        rng = np.random.default_rng(1)
+        rr = radius * np.sqrt(rng.uniform(0.01, 1.0, n))
+        a = rng.uniform(0, 2 * np.pi, n)
+        cur = np.stack([rr * np.cos(a), rr * np.sin(a)], 1).astype(np.float32)
+        prev, w = cur.copy(), np.full(n, weight, np.float32)
+        k, t0 = n, time.perf_counter()
+        cframes = 30
+        with open(os.devnull, "wb") as f:
+            for _ in range(cframes):
+                k2, cur[:k], prev[:k], w[:k], _ = oracle.stars_update(cur[:k], prev[:k], w[:k], level, plim, 0.1, tick)
+                k = k2
+                f.write(b"FRAME\n")
+                f.write(oracle.display(cur[:k], w[:k], width, height, ss, dlim).tobytes())
+        el = time.perf_counter() - t0
+        cpu = {"value": cframes / el, "unit": "frames/s", "cores": oracle.num_threads(), "kind": "port",
+               "sample": f"{cframes} frames of {n:,} stars: the oracle's Stars::update and raster, frames written"}
+    out = {
+        "metric": "frames/s", "value": frames / (api_ms / 1e3), "unit": "frames/s", "n_gpus": 1, "steps": frames,
+        "warmup": args.warmup, "ms_per_step": api_ms / frames, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "generated (the reference's disk model)",
+        "config": {"workload": f"movie: disk script preset, {n:,} stars, {width}x{height}, FMM level {level}, "
+                               f"{frames} frames", "argv": argv},
+        "e2e": {"value": frames / cli_s, "unit": "frames/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": width * height * 3 // 2,
+                "api": "nbfmm_main process, wall clock from start to exit (library load, CUDA start-up, model, "
+                       "frames, file)"},
+        "cpu_baseline": cpu, "gpu_launches": None,
+    }
+    print(json.dumps(out), flush=True)
+
+
 def main():
     args = parse()
     from nbfmm_gb300 import workloads
@@ -478,6 +627,10 @@ def main():
         return run_adjoint(args)
     if args.config == "display_16m" and args.impl == "gb300":
         return run_display(args)
+    if args.config == "models_16m" and args.impl == "gb300":
+        return run_models(args)
+    if args.config == "movie_disk" and args.impl == "gb300":
+        return run_movie(args)
 
     from nbfmm_gb300 import replicas
 
