@@ -272,6 +272,11 @@ int nbfmm_stars_profile_begin(nbfmm_stars* stars, int max_steps);
 /* Ends the session: total P2P milliseconds and number of timed launches. Synchronises. */
 int nbfmm_stars_profile_end(nbfmm_stars* stars, float* p2p_ms_total, int* p2p_launches);
 
+/* Test hook: the next `count` device allocations of the library succeed and every later one fails with
+ * NBFMM_ERR_NOMEM (the frame raster then takes its scratch-free path), until called again; count < 0 turns the
+ * injection off. Lets tests exercise every allocation failure of the create calls without exhausting a GPU. */
+int nbfmm_debug_fail_allocations_after(int count);
+
 /* Number of engine kernels one nbfmm_stars_update(stars, num_steps) call launches. */
 int nbfmm_stars_kernel_launches(nbfmm_stars* stars, int num_steps, long long* launches);
 

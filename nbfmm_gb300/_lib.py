@@ -40,6 +40,7 @@ SIGNATURES = {
     "nbfmm_stars_num_star": (ctypes.c_int, [_vp, _c_int_p]),
     "nbfmm_stars_update": (ctypes.c_int, [_vp, ctypes.c_int, _vp]),
     "nbfmm_stars_prune": (ctypes.c_int, [_vp, _vp]),
+    "nbfmm_debug_fail_allocations_after": (ctypes.c_int, [ctypes.c_int]),
     "nbfmm_device_malloc": (ctypes.c_int, [ctypes.c_ulonglong, ctypes.POINTER(_vp)]),
     "nbfmm_device_free": (ctypes.c_int, [_vp]),
     "nbfmm_memcpy_to_device": (ctypes.c_int, [_vp, _vp, ctypes.c_ulonglong]),

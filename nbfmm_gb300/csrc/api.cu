@@ -8,6 +8,7 @@
 // nbfmm_stars_num_star and the first nbfmm_stars_update of a handle (graph instantiation).
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -34,8 +35,23 @@ int fail(int code, const char* fmt, ...) {
 
 }  // namespace
 
+namespace {
+// Allocations still allowed before injected failures begin; -1: no injection (nbfmm_debug_fail_allocations_after).
+std::atomic<long> g_alloc_budget{-1};
+}  // namespace
+
 // Sets the calling thread's last-error message from another translation unit of the library.
 namespace nbfmm_gb300 {
+
+bool injected_alloc_failure() {
+  long b = g_alloc_budget.load();
+  while (b >= 0) {
+    if (b == 0) return true;
+    if (g_alloc_budget.compare_exchange_weak(b, b - 1)) return false;
+  }
+  return false;
+}
+
 int api_fail(int code, const char* fmt, ...) {
   char buf[512];
   va_list ap;
@@ -478,10 +494,16 @@ int nbfmm_stars_update(nbfmm_stars* stars, int num_steps, void* stream) {
   return stars->update(num_steps, as_stream(stream));
 }
 
+int nbfmm_debug_fail_allocations_after(int count) {
+  g_alloc_budget.store(count < 0 ? -1 : count);
+  return NBFMM_OK;
+}
+
 int nbfmm_device_malloc(unsigned long long bytes, void** gpuptr_out) {
   if (!gpuptr_out) return fail(NBFMM_ERR_INVALID, "null output pointer");
   *gpuptr_out = nullptr;
   if (bytes == 0) return NBFMM_OK;
+  if (injected_alloc_failure()) return fail(NBFMM_ERR_NOMEM, "cudaMalloc of %llu bytes: injected failure", bytes);
   if (cudaMalloc(gpuptr_out, (size_t)bytes) != cudaSuccess) {
     cudaGetLastError();
     *gpuptr_out = nullptr;

@@ -27,6 +27,7 @@
 
 namespace nbfmm_gb300 {
 int api_fail(int code, const char* fmt, ...);
+bool injected_alloc_failure();
 }
 
 using namespace nbfmm_gb300;
@@ -235,6 +236,7 @@ template <typename T>
 int balloc(T** p, size_t count, const char* what) {
   *p = nullptr;
   if (count == 0) count = 1;
+  if (injected_alloc_failure()) return api_fail(NBFMM_ERR_NOMEM, "cudaMalloc(%s): injected failure", what);
   const cudaError_t e = cudaMalloc(reinterpret_cast<void**>(p), count * sizeof(T));
   if (e != cudaSuccess) {
     cudaGetLastError();

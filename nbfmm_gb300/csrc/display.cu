@@ -31,6 +31,7 @@
 
 namespace nbfmm_gb300 {
 int api_fail(int code, const char* fmt, ...);
+bool injected_alloc_failure();
 
 namespace {
 
@@ -320,7 +321,8 @@ void launch_display(const int* d_n, int n_host, int max_n, int width, int height
   const long long slices_ll = (long long)num_sms / bands;
   const int slices = slices_ll > 0 ? (int)slices_ll : 1;
   uint32_t* partial = nullptr;
-  if (cudaFuncSetAttribute(raster_bits_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) != cudaSuccess ||
+  if (injected_alloc_failure() ||
+      cudaFuncSetAttribute(raster_bits_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) != cudaSuccess ||
       cudaMallocAsync(reinterpret_cast<void**>(&partial), (size_t)slices * (size_t)words_total * 4, s) !=
           cudaSuccess) {
     cudaGetLastError();
@@ -420,6 +422,10 @@ int nbfmm_movie_open(nbfmm_stars* stars, const char* path, int width, int height
   for (int k = 0; k < 4; ++k) m->limits[k] = display_limits[k];
   m->bytes = frame_bytes(width, height);
   for (int k = 0; k < 2; ++k) {
+    if (injected_alloc_failure()) {
+      delete m;
+      return api_fail(NBFMM_ERR_NOMEM, "movie: frame buffers: injected failure");
+    }
     if (cudaMalloc(&m->board[k], (size_t)m->bytes) != cudaSuccess ||
         cudaMallocHost(&m->host[k], (size_t)m->bytes) != cudaSuccess ||
         cudaEventCreateWithFlags(&m->copied[k], cudaEventDisableTiming) != cudaSuccess) {

@@ -31,10 +31,15 @@ inline int cuda_check(const char* what) {
     if (_rc != NBFMM_OK) return _rc; \
   } while (0)
 
+// Allocation-failure injection for tests (nbfmm_debug_fail_allocations_after): true when this allocation must
+// fail. Counts every device allocation of the library.
+bool injected_alloc_failure();
+
 template <typename T>
 int dalloc(T** p, size_t count, const char* what) {
   *p = nullptr;
   if (count == 0) count = 1;
+  if (injected_alloc_failure()) return api_fail(NBFMM_ERR_NOMEM, "cudaMalloc(%s): injected failure", what);
   const cudaError_t e = cudaMalloc(reinterpret_cast<void**>(p), count * sizeof(T));
   if (e != cudaSuccess) {
     cudaGetLastError();
