@@ -209,3 +209,35 @@ def test_far_field_of_a_solve_is_bit_exact(engine, orc):
     ref_cells = cube_to_compact(cp, cw, buf)
     np.testing.assert_array_equal(buf["cell"].cpu().numpy()[:, 0:3], ref_cells[:, 0:3])
     np.testing.assert_array_equal(buf["cell_effect"].cpu().numpy(), cube_to_compact(ce, None, buf)[:, 0:2])
+
+
+def test_maximum_size_solve(engine, orc):
+    """The largest solve the API accepts: 2^28 particles at depth 10 (2048 x 2048 leaf cells, ~64 per cell). The
+    cell order is checked over all particles (sorted keys, heads ending at N), and sampled targets against the
+    oracle's full-tree solve."""
+    import torch
+
+    from conftest import guarded_rel_err
+
+    n, level = 1 << 28, 10
+    rng = np.random.default_rng(28)
+    pos = rng.random((n, 2), dtype=np.float32)
+    pos *= np.float32(2.0)
+    pos -= np.float32(1.0)
+    w = rng.random(n, dtype=np.float32)
+    w += np.float32(0.5)
+    lim = (-1.0, -1.0, 1.0, 1.0)
+    s = engine.Solver(level, n, lim, epsilon=1e-3)
+    e = torch.empty(n, 2, device="cuda")
+    s.solve(n, torch.from_numpy(pos).cuda(), torch.from_numpy(w).cuda(), e)
+    torch.cuda.synchronize()
+    b = s.buffers()
+    keys = b["cell_key"][:n]
+    assert bool((keys[1:] >= keys[:-1]).all())
+    head = b["head"]
+    assert int(head[0]) == 0 and int(head[-1]) == n and bool((head[1:] >= head[:-1]).all())
+    targets = np.sort(rng.choice(n, 256, replace=False)).astype(np.int32)
+    got = e[torch.from_numpy(targets).long().cuda()].cpu().numpy()
+    assert np.all(np.isfinite(got))
+    ref = orc.solve_targets(pos, w, level, lim, 1e-3, targets)
+    assert guarded_rel_err(got, ref)[0] < TOL
