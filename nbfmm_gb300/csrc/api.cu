@@ -251,6 +251,7 @@ struct nbfmm_stars {
   float2* state_prev = nullptr;
   float2* sprev = nullptr;
   float4* grave = nullptr;  // final states by original index: two float4 per star (stars.cuh file_grave)
+  uint32_t* order_scratch = nullptr;  // cell_order_kernel's scratch for large cells
   int* counters = nullptr;
   StepCounters sc{};
   cudaStream_t capture_stream = nullptr;
@@ -275,6 +276,7 @@ struct nbfmm_stars {
     NBFMM_TRY(dalloc(&state_prev, n, "state prev"));
     NBFMM_TRY(dalloc(&sprev, n, "sorted prev"));
     NBFMM_TRY(dalloc(&grave, 2 * n, "final states"));
+    NBFMM_TRY(dalloc(&order_scratch, kOrderScratch * n, "cell order scratch"));
     NBFMM_TRY(dalloc(&counters, 8, "step counters"));
     cudaMemset(cur, 0, n * sizeof(float2));
     cudaMemset(prev, 0, n * sizeof(float2));
@@ -317,7 +319,7 @@ struct nbfmm_stars {
     if (cap_b) cudaEventDestroy(cap_b);
     if (capture_stream) cudaStreamDestroy(capture_stream);
     dfree(cur); dfree(prev); dfree(w); dfree(state4); dfree(state_prev); dfree(sprev);
-    dfree(grave); dfree(counters);
+    dfree(grave); dfree(order_scratch); dfree(counters);
     delete solver;
   }
 
@@ -330,7 +332,8 @@ struct nbfmm_stars {
     v.sort(sc.n_cur, v.key_bits, s);
     launch_head(v.skey, sc.n_cur, v.num_cells, v.head, sc.n_alive, s);
     launch_worklist(v.head, v.num_cells, v.work, v.d_work_count(), s);
-    launch_gather_state_p2m(v.geo, v.head, v.perm, state4, state_prev, v.sorted4, sprev, v.cell0(), s);
+    launch_gather_state_ordered(v.head, v.num_cells, v.perm, state4, state_prev, v.sorted4, sprev, v.cell0(),
+                                order_scratch, max_n, s);  // each cell in index order, as the reference sorts
     v.far_field(s);
     P2PArgs a = v.p2p_args();
     a.sprev = sprev;

@@ -303,6 +303,7 @@ struct nbfmm_batch {
   float4* state4 = nullptr;
   float2* state_prev = nullptr;
   float4* grave = nullptr;  // final states by original index: two float4 per star (stars.cuh file_grave)
+  uint32_t* order_scratch = nullptr;  // cell_order_kernel's scratch for large cells
   int* sys_counts = nullptr;  // survivors per system
   int* live_base = nullptr;   // [S + 1] prefix of sys_counts
   int* part_off = nullptr;    // [S + 1] particle ranges
@@ -412,6 +413,7 @@ struct nbfmm_batch {
     BATCH_TRY(balloc(&state4, N, "state"));
     BATCH_TRY(balloc(&state_prev, N, "state prev"));
     BATCH_TRY(balloc(&grave, 2 * (size_t)N, "final states"));
+    BATCH_TRY(balloc(&order_scratch, (size_t)kOrderScratch * N, "cell order scratch"));
     BATCH_TRY(balloc(&sys_counts, (size_t)S, "system counts"));
     BATCH_TRY(balloc(&live_base, (size_t)S + 1, "live prefix"));
     BATCH_TRY(balloc(&part_off, (size_t)S + 1, "particle offsets"));
@@ -458,7 +460,7 @@ struct nbfmm_batch {
     bfree(geo); bfree(sys_of_orig); bfree(cell_base); bfree(dim); bfree(levels); bfree(level_base); bfree(tile_base);
     bfree(keys_a); bfree(vals_a); bfree(keys_b); bfree(vals_b); bfree(counts); bfree(digit_total);
     bfree(head); bfree(work); bfree(sorted4); bfree(sprev); bfree(cell4); bfree(ceff);
-    bfree(cur); bfree(prev); bfree(w); bfree(state4); bfree(state_prev); bfree(grave); bfree(sys_counts);
+    bfree(cur); bfree(prev); bfree(w); bfree(state4); bfree(state_prev); bfree(grave); bfree(order_scratch); bfree(sys_counts);
     bfree(live_base); bfree(part_off); bfree(ints);
   }
 
@@ -494,8 +496,8 @@ struct nbfmm_batch {
     sort(sc.n_cur, key_bits, s);
     launch_head(skey, sc.n_cur, total_leaf, head, sc.n_alive, s);
     launch_worklist(head, total_leaf, work, d_work_count(), s);
-    // gather + P2M over the global leaf space
-    launch_gather_state_p2m_cells(head, total_leaf, perm, state4, state_prev, sorted4, sprev, cell4, s);
+    // gather + P2M over the global leaf space, each cell in index order
+    launch_gather_state_ordered(head, total_leaf, perm, state4, state_prev, sorted4, sprev, cell4, order_scratch, N, s);
     for (int lv = 1; lv < max_levels; ++lv) {
       if (h_level_total[lv] == 0) continue;
       batch_m2m_kernel<<<grid_for(h_level_total[lv], 256, 152 * 8), 256, 0, s>>>(

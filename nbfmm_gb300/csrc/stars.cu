@@ -6,8 +6,10 @@
 // limits to the front and reads the new count back to the host (thrust::find, prune.cu:61).
 //
 // Here the stars live in an internal state kept in the previous step's cell order: state4 = (x, y, m,
-// original index), state_prev = previous positions. A step sorts the state by leaf cell, gathers it, builds
-// the tree and runs P2P with the L2P + Verlet epilogue, which writes the new state in the new cell order.
+// original index), state_prev = previous positions. A step sorts the state by leaf cell, puts each cell back in
+// index order (the reference's predo sorts the caller's arrays, so its cells list their stars by index; the sort
+// here starts from the previous cell order), gathers it, builds the tree and runs P2P with the L2P + Verlet
+// epilogue, which writes the new state in the new cell order.
 // Pruning is folded into the next step's key pass: a star outside the limits gets the key B*B, sorts behind
 // every live star and drops out (head[B*B] is the new count), and its final state is filed under its
 // original index together with its death step. The state of the public arrays (survivors in their previous
@@ -54,30 +56,6 @@ __global__ void keys_from_state_kernel(Geometry g, StepCounters sc, const float4
     }
     keys[i] = key;
     vals[i] = (uint32_t)i;
-  }
-}
-
-__global__ void gather_state_p2m_kernel(int num_cells, const int* __restrict__ head, const uint32_t* __restrict__ perm,
-                                        const float4* __restrict__ state4, const float2* __restrict__ state_prev,
-                                        float4* __restrict__ sorted4, float2* __restrict__ sprev,
-                                        float4* __restrict__ cell0) {
-  const int lane = threadIdx.x & 31;
-  const int nwarps = (gridDim.x * blockDim.x) >> 5;
-  for (int c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; c < num_cells; c += nwarps) {
-    const int h0 = head[c], h1 = head[c + 1];
-    float sx = 0.0f, sy = 0.0f, sw = 0.0f;
-    for (int base = h0; base < h1; base += 32) {
-      const int i = base + lane;
-      float4 q = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-      if (i < h1) {
-        const uint32_t p = perm[i];
-        q = state4[p];
-        sorted4[i] = q;
-        sprev[i] = state_prev[p];
-      }
-      cell_sums_add_chunk(sx, sy, sw, q.x, q.y, q.z, min(32, h1 - base));
-    }
-    if (lane == 0) cell0[c] = centre_of_mass(sx, sy, sw, h1 > h0);
   }
 }
 
@@ -137,6 +115,288 @@ __global__ void prune_keys_kernel(Geometry g, StepCounters sc, const float2* __r
   if (blockIdx.x == 0 && threadIdx.x == 0) *sc.n_import = n;
 }
 
+// ---- Index order inside the leaf cells -------------------------------------------------------------------------
+// The reference's predo sorts the caller's arrays stably by leaf cell (predo.cu:127), so each cell lists its stars
+// by index. A step here sorts the state, which is kept in the previous step's cell order, so the stars a cell
+// received from other cells come as a few increasing runs of indices (one per cell they came from, in that cell's
+// order). The helpers below merge those runs (in a global scratch of kOrderScratch words per particle, at the
+// cell's own offset) for the cells gather_state_ordered_kernel cannot stage in shared memory.
+
+
+struct OrderArrays {
+  uint32_t *key, *val, *key2, *val2;  // index and state slot, ping-pong
+  int *run, *run2, *start;            // run of each element, ping-pong; first element of each run
+};
+
+__device__ __forceinline__ OrderArrays order_arrays(uint32_t* base, int stride) {
+  OrderArrays a;
+  a.key = base;
+  a.val = base + stride;
+  a.key2 = base + 2 * stride;
+  a.val2 = base + 3 * stride;
+  a.run = reinterpret_cast<int*>(base + 4 * stride);
+  a.run2 = reinterpret_cast<int*>(base + 5 * stride);
+  a.start = reinterpret_cast<int*>(base + 6 * stride);
+  return a;
+}
+
+// True when the cell's stars are not in index order (a descent between neighbours).
+__device__ __forceinline__ bool cell_out_of_order(const uint32_t* __restrict__ perm, const float4* __restrict__ state4,
+                                                  int h0, int L, int lane) {
+  uint32_t last = 0u;
+  for (int base = 0; base < L; base += 32) {
+    const int i = base + lane;
+    const uint32_t o = i < L ? (uint32_t)__float_as_int(state4[perm[h0 + i]].w) : 0xffffffffu;
+    uint32_t before = __shfl_up_sync(0xffffffffu, o, 1);
+    if (lane == 0) before = base == 0 ? 0u : last;
+    if (__any_sync(0xffffffffu, i < L && i > 0 && before > o)) return true;
+    last = __shfl_sync(0xffffffffu, o, 31);
+  }
+  return false;
+}
+
+// Loads the cell's (index, slot) pairs and its increasing runs; returns the number of runs. Four chunks of 32 are
+// read per round (their slots, then their indices) to keep several loads in flight.
+__device__ int order_load(const uint32_t* __restrict__ perm, const float4* __restrict__ state4, int h0, int L,
+                          const OrderArrays& a, int lane) {
+  int runs = 0;
+  uint32_t last = 0u;
+  for (int base = 0; base < L; base += 128) {
+    uint32_t slot[4], idx[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const int i = base + 32 * u + lane;
+      slot[u] = i < L ? perm[h0 + i] : 0u;
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const int i = base + 32 * u + lane;
+      idx[u] = i < L ? (uint32_t)__float_as_int(state4[slot[u]].w) : 0xffffffffu;
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const int i = base + 32 * u + lane;
+      if (base + 32 * u >= L) break;  // warp-uniform
+      const uint32_t o = idx[u];
+      uint32_t before = __shfl_up_sync(0xffffffffu, o, 1);
+      if (lane == 0) before = last;
+      const bool starts = i < L && (i == 0 || before > o);
+      const unsigned ballot = __ballot_sync(0xffffffffu, starts);
+      const int r = runs + __popc(ballot & ((2u << lane) - 1u)) - 1;  // (2u << 31) wraps to 0: every lane counted
+      if (i < L) {
+        a.key[i] = o;
+        a.val[i] = slot[u];
+        a.run[i] = r;
+        if (starts) a.start[r] = i;
+      }
+      runs += __popc(ballot);
+      last = __shfl_sync(0xffffffffu, o, 31);
+    }
+  }
+  __syncwarp();
+  return runs;
+}
+
+// Merges the runs into index order; returns the slots in that order (a.val or a.val2). Up to kDirectRuns runs,
+// each element goes straight to its final place, its offset in its own run plus, for every other run, the number
+// of that run's indices below its own (indices are distinct). More runs are merged pairwise, round by round.
+constexpr int kDirectRuns = 16;
+
+__device__ const uint32_t* order_merge(int L, int runs, OrderArrays a, int lane) {
+  if (runs <= kDirectRuns) {
+    for (int i = lane; i < L; i += 32) {
+      const uint32_t k = a.key[i];
+      const int r = a.run[i];
+      int pos = i - a.start[r];
+      for (int q = 0; q < runs; ++q) {
+        if (q == r) continue;
+        int lo = a.start[q], hi = q + 1 < runs ? a.start[q + 1] : L;
+        const int sq = lo;
+        while (lo < hi) {
+          const int mid = (lo + hi) >> 1;
+          if (a.key[mid] < k) lo = mid + 1; else hi = mid;
+        }
+        pos += lo - sq;
+      }
+      a.key2[pos] = k;
+      a.val2[pos] = a.val[i];
+    }
+    __syncwarp();
+    return a.val2;
+  }
+  while (runs > 1) {
+    for (int i = lane; i < L; i += 32) {
+      const uint32_t k = a.key[i];
+      const int r = a.run[i];
+      const int p = r ^ 1;
+      int pos = i;  // an unpaired last run stays in place
+      if (p < runs) {
+        const int sp = a.start[p], ep = p + 1 < runs ? a.start[p + 1] : L;
+        int lo = sp, hi = ep;  // partner elements with a smaller index
+        while (lo < hi) {
+          const int mid = (lo + hi) >> 1;
+          if (a.key[mid] < k) lo = mid + 1; else hi = mid;
+        }
+        const int sr = a.start[r];
+        pos = (sr < sp ? sr : sp) + (i - sr) + (lo - sp);
+      }
+      a.key2[pos] = k;
+      a.val2[pos] = a.val[i];
+      a.run2[pos] = r >> 1;
+    }
+    __syncwarp();
+    const int merged = (runs + 1) >> 1;
+    for (int base = 0; base < merged; base += 32) {  // start[k] = start[2k]
+      const int k = base + lane;
+      const int st = k < merged ? a.start[2 * k] : 0;
+      __syncwarp();
+      if (k < merged) a.start[k] = st;
+      __syncwarp();
+    }
+    uint32_t* t = a.key; a.key = a.key2; a.key2 = t;
+    t = a.val; a.val = a.val2; a.val2 = t;
+    int* u = a.run; a.run = a.run2; a.run2 = u;
+    runs = merged;
+  }
+  return a.val;
+}
+
+// Gather + P2M of a step in the reference's order: per leaf cell, the stars in index order (the runs merged when
+// the sort left them out of order), their state gathered into cell order and the cell's centre of mass summed in
+// that order (p2m.cu:36-46). The order of a cell of up to kStageCap stars is worked out in shared memory (index,
+// slot and run of each star, 14 bytes a star, so that many warps fit on an SM); its state is then gathered in the
+// final order, from lines the first pass has just brought into the caches. A larger cell, or one of more than
+// kDirectRuns runs, is ordered in the global scratch at its own offset.
+constexpr int kStageWarps = 4;
+constexpr int kStageCap = 320;
+
+struct StageArrays {
+  uint32_t key[kStageCap], slot[kStageCap];
+  unsigned short run[kStageCap], start[kStageCap], src[kStageCap];
+};
+
+__global__ void __launch_bounds__(kStageWarps * 32) gather_state_ordered_kernel(
+    int num_cells, const int* __restrict__ head, const uint32_t* __restrict__ perm, const float4* __restrict__ state4,
+    const float2* __restrict__ state_prev, float4* __restrict__ sorted4, float2* __restrict__ sprev,
+    float4* __restrict__ cell0, uint32_t* __restrict__ scratch, int max_n) {
+  __shared__ StageArrays stage[kStageWarps];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  StageArrays& st = stage[warp];
+  const int warps = gridDim.x * kStageWarps;
+  for (int c = blockIdx.x * kStageWarps + warp; c < num_cells; c += warps) {
+    const int h0 = head[c], h1 = head[c + 1], L = h1 - h0;
+    float sx = 0.0f, sy = 0.0f, sw = 0.0f;
+    bool staged = L <= kStageCap;
+    int runs = 1;
+    if (staged) {
+      // Stage the cell's order, four chunks of 32 in flight: slots, then indices.
+      uint32_t last = 0u;
+      runs = 0;
+      for (int base = 0; base < L; base += 128) {
+        uint32_t slot[4], idx[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          const int i = base + 32 * u + lane;
+          slot[u] = i < L ? perm[h0 + i] : 0u;
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          const int i = base + 32 * u + lane;
+          idx[u] = i < L ? (uint32_t)__float_as_int(state4[slot[u]].w) : 0xffffffffu;
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          if (base + 32 * u >= L) break;  // warp-uniform
+          const int i = base + 32 * u + lane;
+          const uint32_t o = idx[u];
+          uint32_t before = __shfl_up_sync(0xffffffffu, o, 1);
+          if (lane == 0) before = last;
+          const bool starts = i < L && (i == 0 || before > o);
+          const unsigned ballot = __ballot_sync(0xffffffffu, starts);
+          const int r = runs + __popc(ballot & ((2u << lane) - 1u)) - 1;  // (2u << 31) wraps to 0
+          if (i < L) {
+            st.key[i] = o;
+            st.slot[i] = slot[u];
+            st.run[i] = (unsigned short)r;
+            if (starts && r < kStageCap) st.start[r] = (unsigned short)i;
+          }
+          runs += __popc(ballot);
+          last = __shfl_sync(0xffffffffu, o, 31);
+        }
+      }
+      __syncwarp();
+      if (runs > kDirectRuns) {
+        staged = false;  // too many runs for direct ranks: order in the scratch below
+      } else if (runs > 1) {
+        // Direct ranks: src[final position] = staged element.
+        for (int i = lane; i < L; i += 32) {
+          const uint32_t k = st.key[i];
+          const int r = st.run[i];
+          int pos = i - st.start[r];
+          for (int q = 0; q < runs; ++q) {
+            if (q == r) continue;
+            int lo = st.start[q], hi = q + 1 < runs ? st.start[q + 1] : L;
+            const int sq = lo;
+            while (lo < hi) {
+              const int mid = (lo + hi) >> 1;
+              if (st.key[mid] < k) lo = mid + 1; else hi = mid;
+            }
+            pos += lo - sq;
+          }
+          st.src[pos] = (unsigned short)i;
+        }
+        __syncwarp();
+      }
+    }
+    if (staged) {
+      for (int base = 0; base < L; base += 128) {  // four chunks of 32 in flight, summed in order
+        float4 q[4];
+        float2 pv[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          const int j = base + 32 * u + lane;
+          q[u] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+          pv[u] = make_float2(0.0f, 0.0f);
+          if (j < L) {
+            const uint32_t p = st.slot[runs > 1 ? st.src[j] : j];
+            q[u] = state4[p];
+            pv[u] = state_prev[p];
+          }
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          const int j = base + 32 * u + lane;
+          if (base + 32 * u >= L) break;  // warp-uniform
+          if (j < L) {
+            sorted4[h0 + j] = q[u];
+            sprev[h0 + j] = pv[u];
+          }
+          cell_sums_add_chunk(sx, sy, sw, q[u].x, q[u].y, q[u].z, min(32, L - base - 32 * u));
+        }
+      }
+    } else {
+      const uint32_t* order = perm + h0;
+      if (L >= 2 && cell_out_of_order(perm, state4, h0, L, lane)) {
+        const OrderArrays a = order_arrays(scratch + h0, max_n);
+        order = order_merge(L, order_load(perm, state4, h0, L, a, lane), a, lane);
+      }
+      for (int base = 0; base < L; base += 32) {
+        const int i = base + lane;
+        float4 q = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        if (i < L) {
+          const uint32_t p = order[i];
+          q = state4[p];
+          sorted4[h0 + i] = q;
+          sprev[h0 + i] = state_prev[p];
+        }
+        cell_sums_add_chunk(sx, sy, sw, q.x, q.y, q.z, min(32, L - base));
+      }
+    }
+    if (lane == 0) cell0[c] = centre_of_mass(sx, sy, sw, h1 > h0);
+    __syncwarp();  // the staging area is free for the next cell
+  }
+}
+
 int grid_for(long long n, int threads, int cap) {
   long long g = (n + threads - 1) / threads;
   if (g < 1) g = 1;
@@ -160,21 +420,6 @@ void launch_keys_from_state(const Geometry& g, const StepCounters& sc, const flo
                                                                              vals, grave);
 }
 
-void launch_gather_state_p2m(const Geometry& g, const int* head, const uint32_t* perm, const float4* state4,
-                             const float2* state_prev, float4* sorted4, float2* sprev, float4* cell0,
-                             cudaStream_t stream) {
-  const int cells = g.base_dim * g.base_dim;
-  gather_state_p2m_kernel<<<grid_for((long long)cells * 32, 256, 152 * 16), 256, 0, stream>>>(
-      cells, head, perm, state4, state_prev, sorted4, sprev, cell0);
-}
-
-void launch_gather_state_p2m_cells(const int* head, int num_cells, const uint32_t* perm, const float4* state4,
-                                   const float2* state_prev, float4* sorted4, float2* sprev, float4* cell0,
-                                   cudaStream_t stream) {
-  gather_state_p2m_kernel<<<grid_for((long long)num_cells * 32, 256, 152 * 16), 256, 0, stream>>>(
-      num_cells, head, perm, state4, state_prev, sorted4, sprev, cell0);
-}
-
 void launch_finish_step(const StepCounters& sc, cudaStream_t stream) { finish_step_kernel<<<1, 1, 0, stream>>>(sc); }
 
 void launch_export_fate(const Geometry& g, const StepCounters& sc, const float4* state4, const float2* state_prev,
@@ -190,6 +435,14 @@ void launch_fate_keys(const StepCounters& sc, const float4* grave, uint32_t* key
 void launch_export_gather(const StepCounters& sc, const uint32_t* order, const float4* grave, float2* cur,
                           float2* prev, float* w, int max_n, cudaStream_t stream) {
   export_gather_kernel<<<grid_for(max_n, 256, 152 * 16), 256, 0, stream>>>(sc, order, grave, cur, prev, w);
+}
+
+void launch_gather_state_ordered(const int* head, int num_cells, const uint32_t* perm, const float4* state4,
+                                 const float2* state_prev, float4* sorted4, float2* sprev, float4* cell0,
+                                 uint32_t* scratch, int max_n, cudaStream_t stream) {
+  gather_state_ordered_kernel<<<grid_for((long long)num_cells * 32, kStageWarps * 32, 152 * 8), kStageWarps * 32, 0,
+                                stream>>>(num_cells, head, perm, state4, state_prev, sorted4, sprev, cell0, scratch,
+                                          max_n);
 }
 
 void launch_prune_keys(const Geometry& g, const StepCounters& sc, const float2* cur, const float2* prev,

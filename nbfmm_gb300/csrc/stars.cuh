@@ -36,13 +36,6 @@ void launch_import(const StepCounters& sc, const float2* cur, const float2* prev
 void launch_keys_from_state(const Geometry& g, const StepCounters& sc, const float4* state4, const float2* state_prev,
                             uint32_t dead_key, uint32_t* keys, uint32_t* vals, float4* grave, int max_n,
                             cudaStream_t stream);
-void launch_gather_state_p2m(const Geometry& g, const int* head, const uint32_t* perm, const float4* state4,
-                             const float2* state_prev, float4* sorted4, float2* sprev, float4* cell0,
-                             cudaStream_t stream);
-// Same as launch_gather_state_p2m over `num_cells` leaf cells of any layout (the batched form's global space).
-void launch_gather_state_p2m_cells(const int* head, int num_cells, const uint32_t* perm, const float4* state4,
-                                   const float2* state_prev, float4* sorted4, float2* sprev, float4* cell0,
-                                   cudaStream_t stream);
 void launch_finish_step(const StepCounters& sc, cudaStream_t stream);
 void launch_export_fate(const Geometry& g, const StepCounters& sc, const float4* state4, const float2* state_prev,
                         float4* grave, int max_n, cudaStream_t stream);
@@ -50,6 +43,15 @@ void launch_fate_keys(const StepCounters& sc, const float4* grave, uint32_t* key
                       cudaStream_t stream);
 void launch_export_gather(const StepCounters& sc, const uint32_t* order, const float4* grave, float2* cur,
                           float2* prev, float* w, int max_n, cudaStream_t stream);
+
+// The gather + P2M of a step over `num_cells` leaf cells of any layout (the batched form's global space too): the
+// state gathered into cell order with every leaf cell in index order, the order the reference's stable sort of the
+// caller's arrays gives (the step's sort keeps the previous cell order instead), and each cell's centre of mass
+// summed in that order. scratch holds kOrderScratch * max_n words for cells too large for shared memory.
+constexpr int kOrderScratch = 7;
+void launch_gather_state_ordered(const int* head, int num_cells, const uint32_t* perm, const float4* state4,
+                                 const float2* state_prev, float4* sorted4, float2* sprev, float4* cell0,
+                                 uint32_t* scratch, int max_n, cudaStream_t stream);
 
 // Stars::prune on the public arrays (prune.cu:28-62), step 1: n_import = num_star, keys 1 for the stars outside
 // the limits and 0 otherwise, vals the identity, and a copy of the arrays into grave records to gather back from.

@@ -116,3 +116,28 @@ def test_initialize_forwards_tick_and_state(engine):
     torch.cuda.synchronize()
     assert st.num_star_ == 256
     assert torch.all(torch.isfinite(st.gpuptr_position_cur_))
+
+
+@pytest.mark.parametrize("level", [3, 5])
+def test_grouping_of_steps_into_calls_does_not_matter(engine, level):
+    """Stars crossing leaf cells at every step: K steps in one call equal K calls of one step, bit for bit. Each
+    call starts from the caller's order, so this holds only if every step orders each leaf cell by index, as the
+    reference's predo does (a stable sort of the caller's arrays), whatever cells the stars came from."""
+    import torch
+
+    rng = np.random.default_rng(level)
+    n = 6000
+    cur = rng.uniform(-0.8, 0.8, (n, 2)).astype(np.float32)
+    prev = (cur - rng.uniform(-6e-3, 6e-3, (n, 2))).astype(np.float32)  # ~20-40% of the stars change cells each step
+    w = (rng.uniform(0.5, 1.5, n) / n).astype(np.float32)
+    lim, tick, eps = (-1.0, -1.0, 1.0, 1.0), 1.0, 1e-3
+    a = make_stars(engine, cur, prev, w, level, lim, tick, eps)
+    b = make_stars(engine, cur, prev, w, level, lim, tick, eps)
+    a.update(8)
+    for _ in range(8):
+        b.update(1)
+    torch.cuda.synchronize()
+    assert a.num_star_ == b.num_star_
+    assert torch.equal(a.gpuptr_position_cur_, b.gpuptr_position_cur_)
+    assert torch.equal(a.gpuptr_position_pre_, b.gpuptr_position_pre_)
+    assert torch.equal(a.gpuptr_weight_, b.gpuptr_weight_)
