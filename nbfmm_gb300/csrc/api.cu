@@ -251,7 +251,7 @@ struct nbfmm_stars {
   float2* state_prev = nullptr;
   float2* sprev = nullptr;
   float4* grave = nullptr;  // final states by original index: two float4 per star (stars.cuh file_grave)
-  uint32_t* order_scratch = nullptr;  // cell_order_kernel's scratch for large cells
+  uint32_t* order_scratch = nullptr;  // gather_state_ordered_kernel's scratch for large cells
   int* counters = nullptr;
   StepCounters sc{};
   cudaStream_t capture_stream = nullptr;

@@ -303,7 +303,7 @@ struct nbfmm_batch {
   float4* state4 = nullptr;
   float2* state_prev = nullptr;
   float4* grave = nullptr;  // final states by original index: two float4 per star (stars.cuh file_grave)
-  uint32_t* order_scratch = nullptr;  // cell_order_kernel's scratch for large cells
+  uint32_t* order_scratch = nullptr;  // gather_state_ordered_kernel's scratch for large cells
   int* sys_counts = nullptr;  // survivors per system
   int* live_base = nullptr;   // [S + 1] prefix of sys_counts
   int* part_off = nullptr;    // [S + 1] particle ranges

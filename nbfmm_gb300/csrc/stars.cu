@@ -122,7 +122,6 @@ __global__ void prune_keys_kernel(Geometry g, StepCounters sc, const float2* __r
 // order). The helpers below merge those runs (in a global scratch of kOrderScratch words per particle, at the
 // cell's own offset) for the cells gather_state_ordered_kernel cannot stage in shared memory.
 
-
 struct OrderArrays {
   uint32_t *key, *val, *key2, *val2;  // index and state slot, ping-pong
   int *run, *run2, *start;            // run of each element, ping-pong; first element of each run
