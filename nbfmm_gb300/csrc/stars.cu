@@ -41,7 +41,7 @@ __global__ void import_kernel(StepCounters sc, const float2* __restrict__ cur, c
 __global__ void keys_from_state_kernel(Geometry g, StepCounters sc, const float4* __restrict__ state4,
                                        const float2* __restrict__ state_prev, uint32_t dead_key,
                                        uint32_t* __restrict__ keys, uint32_t* __restrict__ vals,
-                                       float4* __restrict__ grave) {
+                                       float4* __restrict__ grave, uint32_t* __restrict__ slot_index) {
   const int n = *sc.n_cur;
   const int prune = *sc.prune;
   const int death_rank = *sc.num_steps + 1 - (*sc.step - 1);  // later deaths first in the final order
@@ -56,6 +56,7 @@ __global__ void keys_from_state_kernel(Geometry g, StepCounters sc, const float4
     }
     keys[i] = key;
     vals[i] = (uint32_t)i;
+    slot_index[i] = (uint32_t)__float_as_int(p.w);
   }
 }
 
@@ -140,12 +141,12 @@ __device__ __forceinline__ OrderArrays order_arrays(uint32_t* base, int stride) 
 }
 
 // True when the cell's stars are not in index order (a descent between neighbours).
-__device__ __forceinline__ bool cell_out_of_order(const uint32_t* __restrict__ perm, const float4* __restrict__ state4,
-                                                  int h0, int L, int lane) {
+__device__ __forceinline__ bool cell_out_of_order(const uint32_t* __restrict__ perm,
+                                                  const uint32_t* __restrict__ slot_index, int h0, int L, int lane) {
   uint32_t last = 0u;
   for (int base = 0; base < L; base += 32) {
     const int i = base + lane;
-    const uint32_t o = i < L ? (uint32_t)__float_as_int(state4[perm[h0 + i]].w) : 0xffffffffu;
+    const uint32_t o = i < L ? slot_index[perm[h0 + i]] : 0xffffffffu;
     uint32_t before = __shfl_up_sync(0xffffffffu, o, 1);
     if (lane == 0) before = base == 0 ? 0u : last;
     if (__any_sync(0xffffffffu, i < L && i > 0 && before > o)) return true;
@@ -156,7 +157,7 @@ __device__ __forceinline__ bool cell_out_of_order(const uint32_t* __restrict__ p
 
 // Loads the cell's (index, slot) pairs and its increasing runs; returns the number of runs. Four chunks of 32 are
 // read per round (their slots, then their indices) to keep several loads in flight.
-__device__ int order_load(const uint32_t* __restrict__ perm, const float4* __restrict__ state4, int h0, int L,
+__device__ int order_load(const uint32_t* __restrict__ perm, const uint32_t* __restrict__ slot_index, int h0, int L,
                           const OrderArrays& a, int lane) {
   int runs = 0;
   uint32_t last = 0u;
@@ -170,7 +171,7 @@ __device__ int order_load(const uint32_t* __restrict__ perm, const float4* __res
 #pragma unroll
     for (int u = 0; u < 4; ++u) {
       const int i = base + 32 * u + lane;
-      idx[u] = i < L ? (uint32_t)__float_as_int(state4[slot[u]].w) : 0xffffffffu;
+      idx[u] = i < L ? slot_index[slot[u]] : 0xffffffffu;
     }
 #pragma unroll
     for (int u = 0; u < 4; ++u) {
@@ -262,122 +263,216 @@ __device__ const uint32_t* order_merge(int L, int runs, OrderArrays a, int lane)
 
 // Gather + P2M of a step in the reference's order: per leaf cell, the stars in index order (the runs merged when
 // the sort left them out of order), their state gathered into cell order and the cell's centre of mass summed in
-// that order (p2m.cu:36-46). The order of a cell of up to kStageCap stars is worked out in shared memory (index,
-// slot and run of each star, 14 bytes a star, so that many warps fit on an SM); its state is then gathered in the
-// final order, from lines the first pass has just brought into the caches. A larger cell, or one of more than
-// kDirectRuns runs, is ordered in the global scratch at its own offset.
+// that order (p2m.cu:36-46). A warp takes a cell of up to kStageCap stars in one round: it loads the slots, then
+// every slot's state (which carries the index) and previous position at once into registers. A cell already in
+// index order is written out as loaded. Otherwise each star's final place is worked out from the indices staged
+// in shared memory -- usually one long run (the residents) and a few other stars (the arrivals), which are
+// sorted across the lanes, placed into the long run by binary search and shift the residents by a prefix count;
+// else by its rank across all runs -- the star is written there, and the centre of mass is summed from a
+// shared-memory copy in final order. A larger cell, or one of more than kDirectRuns runs and more than 32
+// arrivals, is ordered in the global scratch at its own offset and gathered from the state.
 constexpr int kStageWarps = 4;
-constexpr int kStageCap = 320;
+constexpr int kStageChunks = 10;                 // chunks of 32 stars held in registers
+constexpr int kStageCap = 32 * kStageChunks;     // 320
 
 struct StageArrays {
-  uint32_t key[kStageCap], slot[kStageCap];
-  unsigned short run[kStageCap], start[kStageCap], src[kStageCap];
+  uint32_t key[kStageCap];
+  float xs[kStageCap], ys[kStageCap], ms[kStageCap];
+  int shift[kStageCap + 1];
+  unsigned short run[kStageCap], start[kStageCap], dest[kStageCap];
 };
 
-__global__ void __launch_bounds__(kStageWarps * 32) gather_state_ordered_kernel(
+// Sorts one (key, value) pair per lane into ascending key order across the warp (bitonic network).
+__device__ __forceinline__ void warp_sort_pairs(uint32_t& k, int& v, int lane) {
+#pragma unroll
+  for (int size = 2; size <= 32; size <<= 1) {
+#pragma unroll
+    for (int stride = size >> 1; stride > 0; stride >>= 1) {
+      const uint32_t ok = __shfl_xor_sync(0xffffffffu, k, stride);
+      const int ov = __shfl_xor_sync(0xffffffffu, v, stride);
+      const bool ascending = (lane & size) == 0 || size == 32;
+      const bool lower = (lane & stride) == 0;
+      const bool take = (lower == ascending) ? ok < k : ok > k;
+      if (take) {
+        k = ok;
+        v = ov;
+      }
+    }
+  }
+}
+
+__global__ void __launch_bounds__(kStageWarps * 32, 4) gather_state_ordered_kernel(
     int num_cells, const int* __restrict__ head, const uint32_t* __restrict__ perm, const float4* __restrict__ state4,
     const float2* __restrict__ state_prev, float4* __restrict__ sorted4, float2* __restrict__ sprev,
     float4* __restrict__ cell0, uint32_t* __restrict__ scratch, int max_n) {
   __shared__ StageArrays stage[kStageWarps];
+  const uint32_t* __restrict__ slot_index = order_slot_index(scratch, max_n);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   StageArrays& st = stage[warp];
   const int warps = gridDim.x * kStageWarps;
   for (int c = blockIdx.x * kStageWarps + warp; c < num_cells; c += warps) {
     const int h0 = head[c], h1 = head[c + 1], L = h1 - h0;
     float sx = 0.0f, sy = 0.0f, sw = 0.0f;
-    bool staged = L <= kStageCap;
-    int runs = 1;
-    if (staged) {
-      // Stage the cell's order, four chunks of 32 in flight: slots, then indices.
-      uint32_t last = 0u;
-      runs = 0;
-      for (int base = 0; base < L; base += 128) {
-        uint32_t slot[4], idx[4];
+    bool done = false;
+    if (L <= kStageCap) {
+      uint32_t slot[kStageChunks], idx[kStageChunks];
+      float4 q[kStageChunks];
+      float2 pv[kStageChunks];
 #pragma unroll
-        for (int u = 0; u < 4; ++u) {
-          const int i = base + 32 * u + lane;
-          slot[u] = i < L ? perm[h0 + i] : 0u;
-        }
+      for (int u = 0; u < kStageChunks; ++u) {
+        const int i = 32 * u + lane;
+        slot[u] = i < L ? perm[h0 + i] : 0u;
+      }
 #pragma unroll
-        for (int u = 0; u < 4; ++u) {
-          const int i = base + 32 * u + lane;
-          idx[u] = i < L ? (uint32_t)__float_as_int(state4[slot[u]].w) : 0xffffffffu;
-        }
-#pragma unroll
-        for (int u = 0; u < 4; ++u) {
-          if (base + 32 * u >= L) break;  // warp-uniform
-          const int i = base + 32 * u + lane;
-          const uint32_t o = idx[u];
-          uint32_t before = __shfl_up_sync(0xffffffffu, o, 1);
-          if (lane == 0) before = last;
-          const bool starts = i < L && (i == 0 || before > o);
-          const unsigned ballot = __ballot_sync(0xffffffffu, starts);
-          const int r = runs + __popc(ballot & ((2u << lane) - 1u)) - 1;  // (2u << 31) wraps to 0
-          if (i < L) {
-            st.key[i] = o;
-            st.slot[i] = slot[u];
-            st.run[i] = (unsigned short)r;
-            if (starts && r < kStageCap) st.start[r] = (unsigned short)i;
-          }
-          runs += __popc(ballot);
-          last = __shfl_sync(0xffffffffu, o, 31);
+      for (int u = 0; u < kStageChunks; ++u) {
+        const int i = 32 * u + lane;
+        idx[u] = 0xffffffffu;
+        q[u] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        pv[u] = make_float2(0.0f, 0.0f);
+        if (i < L) {
+          q[u] = state4[slot[u]];
+          pv[u] = state_prev[slot[u]];
+          idx[u] = (uint32_t)__float_as_int(q[u].w);  // the state carries the index
         }
       }
+      // Runs of increasing index.
+      int runs = 0;
+      uint32_t last = 0u;
+#pragma unroll
+      for (int u = 0; u < kStageChunks; ++u) {
+        if (32 * u >= L) break;  // warp-uniform
+        const int i = 32 * u + lane;
+        uint32_t before = __shfl_up_sync(0xffffffffu, idx[u], 1);
+        if (lane == 0) before = last;
+        const bool starts = i < L && (i == 0 || before > idx[u]);
+        const unsigned ballot = __ballot_sync(0xffffffffu, starts);
+        const int r = runs + __popc(ballot & ((2u << lane) - 1u)) - 1;  // (2u << 31) wraps to 0
+        if (i < L) {
+          st.key[i] = idx[u];
+          st.run[i] = (unsigned short)r;
+          if (starts) st.start[r] = (unsigned short)i;
+        }
+        runs += __popc(ballot);
+        last = __shfl_sync(0xffffffffu, idx[u], 31);
+      }
       __syncwarp();
-      if (runs > kDirectRuns) {
-        staged = false;  // too many runs for direct ranks: order in the scratch below
-      } else if (runs > 1) {
-        // Direct ranks: src[final position] = staged element.
-        for (int i = lane; i < L; i += 32) {
-          const uint32_t k = st.key[i];
-          const int r = st.run[i];
-          int pos = i - st.start[r];
-          for (int q = 0; q < runs; ++q) {
-            if (q == r) continue;
-            int lo = st.start[q], hi = q + 1 < runs ? st.start[q + 1] : L;
-            const int sq = lo;
+      if (runs <= 1) {
+#pragma unroll
+        for (int u = 0; u < kStageChunks; ++u) {
+          if (32 * u >= L) break;
+          const int i = 32 * u + lane;
+          if (i < L) {
+            sorted4[h0 + i] = q[u];
+            sprev[h0 + i] = pv[u];
+          }
+          cell_sums_add_chunk(sx, sy, sw, q[u].x, q[u].y, q[u].z, min(32, L - 32 * u));
+        }
+        done = true;
+      } else {
+        // dest[i] = final place of staged star i. The common case: one long run (the cell's residents) and at
+        // most 32 other stars (the arrivals), which are sorted across the lanes, placed into the long run by
+        // binary search, and shift the long run's stars by a prefix count.
+        int best_len = -1, best_r = 0;
+        for (int r = lane; r < runs; r += 32) {
+          const int len = (r + 1 < runs ? st.start[r + 1] : L) - st.start[r];
+          if (len > best_len) {
+            best_len = len;
+            best_r = r;
+          }
+        }
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) {
+          const int ol = __shfl_xor_sync(0xffffffffu, best_len, off);
+          const int orr = __shfl_xor_sync(0xffffffffu, best_r, off);
+          if (ol > best_len || (ol == best_len && orr < best_r)) {
+            best_len = ol;
+            best_r = orr;
+          }
+        }
+        const int s0 = st.start[best_r], e0 = s0 + best_len, m = L - best_len;
+        bool placed = false;
+        if (m <= 32) {
+          const int ia = lane < s0 ? lane : e0 + (lane - s0);  // the stars outside the long run
+          uint32_t k = lane < m ? st.key[ia] : 0xffffffffu;
+          int v = lane < m ? ia : -1;
+          warp_sort_pairs(k, v, lane);
+          int p = 0;
+          if (lane < m) {
+            int lo = s0, hi = e0;
             while (lo < hi) {
               const int mid = (lo + hi) >> 1;
               if (st.key[mid] < k) lo = mid + 1; else hi = mid;
             }
-            pos += lo - sq;
+            p = lo - s0;
+            st.dest[v] = (unsigned short)(p + lane);
           }
-          st.src[pos] = (unsigned short)i;
+          for (int o = lane; o <= best_len; o += 32) st.shift[o] = 0;
+          __syncwarp();
+          if (lane < m) atomicAdd(&st.shift[p], 1);
+          __syncwarp();
+          int carry = 0;
+          for (int base = 0; base < best_len; base += 32) {  // inclusive prefix of the insertions
+            const int o = base + lane;
+            int x = o < best_len ? st.shift[o] : 0;
+#pragma unroll
+            for (int off = 1; off < 32; off <<= 1) {
+              const int y = __shfl_up_sync(0xffffffffu, x, off);
+              if (lane >= off) x += y;
+            }
+            if (o < best_len) st.dest[s0 + o] = (unsigned short)(o + carry + x);
+            carry += __shfl_sync(0xffffffffu, x, 31);
+          }
+          placed = true;
+        } else if (runs <= kDirectRuns) {  // direct ranks
+          for (int i = lane; i < L; i += 32) {
+            const uint32_t k = st.key[i];
+            const int r = st.run[i];
+            int pos = i - st.start[r];
+            for (int t = 0; t < runs; ++t) {
+              if (t == r) continue;
+              int lo = st.start[t], hi = t + 1 < runs ? st.start[t + 1] : L;
+              const int s1 = lo;
+              while (lo < hi) {
+                const int mid = (lo + hi) >> 1;
+                if (st.key[mid] < k) lo = mid + 1; else hi = mid;
+              }
+              pos += lo - s1;
+            }
+            st.dest[i] = (unsigned short)pos;
+          }
+          placed = true;
         }
-        __syncwarp();
+        if (placed) {
+          __syncwarp();
+#pragma unroll
+          for (int u = 0; u < kStageChunks; ++u) {
+            if (32 * u >= L) break;
+            const int i = 32 * u + lane;
+            if (i < L) {
+              const int pos = st.dest[i];
+              sorted4[h0 + pos] = q[u];
+              sprev[h0 + pos] = pv[u];
+              st.xs[pos] = q[u].x;
+              st.ys[pos] = q[u].y;
+              st.ms[pos] = q[u].z;
+            }
+          }
+          __syncwarp();
+          for (int base = 0; base < L; base += 32) {
+            const int j = base + lane;
+            const bool in = j < L;
+            cell_sums_add_chunk(sx, sy, sw, in ? st.xs[j] : 0.0f, in ? st.ys[j] : 0.0f, in ? st.ms[j] : 0.0f,
+                                min(32, L - base));
+          }
+          done = true;
+        }
       }
     }
-    if (staged) {
-      for (int base = 0; base < L; base += 128) {  // four chunks of 32 in flight, summed in order
-        float4 q[4];
-        float2 pv[4];
-#pragma unroll
-        for (int u = 0; u < 4; ++u) {
-          const int j = base + 32 * u + lane;
-          q[u] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-          pv[u] = make_float2(0.0f, 0.0f);
-          if (j < L) {
-            const uint32_t p = st.slot[runs > 1 ? st.src[j] : j];
-            q[u] = state4[p];
-            pv[u] = state_prev[p];
-          }
-        }
-#pragma unroll
-        for (int u = 0; u < 4; ++u) {
-          const int j = base + 32 * u + lane;
-          if (base + 32 * u >= L) break;  // warp-uniform
-          if (j < L) {
-            sorted4[h0 + j] = q[u];
-            sprev[h0 + j] = pv[u];
-          }
-          cell_sums_add_chunk(sx, sy, sw, q[u].x, q[u].y, q[u].z, min(32, L - base - 32 * u));
-        }
-      }
-    } else {
+    if (!done) {  // a cell larger than the stage, or of many runs
       const uint32_t* order = perm + h0;
-      if (L >= 2 && cell_out_of_order(perm, state4, h0, L, lane)) {
+      if (L >= 2 && cell_out_of_order(perm, slot_index, h0, L, lane)) {
         const OrderArrays a = order_arrays(scratch + h0, max_n);
-        order = order_merge(L, order_load(perm, state4, h0, L, a, lane), a, lane);
+        order = order_merge(L, order_load(perm, slot_index, h0, L, a, lane), a, lane);
       }
       for (int base = 0; base < L; base += 32) {
         const int i = base + lane;
@@ -413,10 +508,10 @@ void launch_import(const StepCounters& sc, const float2* cur, const float2* prev
 }
 
 void launch_keys_from_state(const Geometry& g, const StepCounters& sc, const float4* state4, const float2* state_prev,
-                            uint32_t dead_key, uint32_t* keys, uint32_t* vals, float4* grave, int max_n,
-                            cudaStream_t stream) {
+                            uint32_t dead_key, uint32_t* keys, uint32_t* vals, float4* grave, uint32_t* slot_index,
+                            int max_n, cudaStream_t stream) {
   keys_from_state_kernel<<<grid_for(max_n, 256, 152 * 16), 256, 0, stream>>>(g, sc, state4, state_prev, dead_key, keys,
-                                                                             vals, grave);
+                                                                             vals, grave, slot_index);
 }
 
 void launch_finish_step(const StepCounters& sc, cudaStream_t stream) { finish_step_kernel<<<1, 1, 0, stream>>>(sc); }
@@ -439,7 +534,7 @@ void launch_export_gather(const StepCounters& sc, const uint32_t* order, const f
 void launch_gather_state_ordered(const int* head, int num_cells, const uint32_t* perm, const float4* state4,
                                  const float2* state_prev, float4* sorted4, float2* sprev, float4* cell0,
                                  uint32_t* scratch, int max_n, cudaStream_t stream) {
-  gather_state_ordered_kernel<<<grid_for((long long)num_cells * 32, kStageWarps * 32, 152 * 8), kStageWarps * 32, 0,
+  gather_state_ordered_kernel<<<grid_for((long long)num_cells * 32, kStageWarps * 32, 152 * 4), kStageWarps * 32, 0,
                                 stream>>>(num_cells, head, perm, state4, state_prev, sorted4, sprev, cell0, scratch,
                                           max_n);
 }
