@@ -328,8 +328,7 @@ struct nbfmm_stars {
   void enqueue_step(cudaStream_t s) {
     nbfmm_solver& v = *solver;
     const uint32_t dead = (uint32_t)v.num_cells;
-    launch_keys_from_state(v.geo, sc, state4, state_prev, dead, v.keys_a, v.vals_a, grave,
-                           order_slot_index(order_scratch, max_n), max_n, s);
+    launch_keys_from_state(v.geo, sc, state4, state_prev, dead, v.keys_a, v.vals_a, grave, max_n, s);
     v.sort(sc.n_cur, v.key_bits, s);
     launch_head(v.skey, sc.n_cur, v.num_cells, v.head, sc.n_alive, s);
     launch_worklist(v.head, v.num_cells, v.work, v.d_work_count(), s);

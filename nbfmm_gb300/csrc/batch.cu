@@ -109,7 +109,7 @@ __global__ void batch_import_kernel(BatchDevice bd, StepCounters sc, const int* 
 __global__ void batch_keys_kernel(BatchDevice bd, StepCounters sc, const float4* __restrict__ state4,
                                   const float2* __restrict__ state_prev, uint32_t dead_key,
                                   uint32_t* __restrict__ keys, uint32_t* __restrict__ vals,
-                                  float4* __restrict__ grave, uint32_t* __restrict__ slot_index) {
+                                  float4* __restrict__ grave) {
   const int n = *sc.n_cur;
   const int prune = *sc.prune;
   const int death_rank = *sc.num_steps + 1 - (*sc.step - 1);
@@ -127,7 +127,6 @@ __global__ void batch_keys_kernel(BatchDevice bd, StepCounters sc, const float4*
     }
     keys[i] = key;
     vals[i] = (uint32_t)i;
-    slot_index[i] = (uint32_t)orig;
   }
 }
 
@@ -493,8 +492,7 @@ struct nbfmm_batch {
   void enqueue_step(cudaStream_t s) {
     const int N = std::max(n, 1);
     batch_keys_kernel<<<grid_for(N, 256, 152 * 16), 256, 0, s>>>(device(), sc, state4, state_prev,
-                                                                (uint32_t)total_leaf, keys_a, vals_a, grave,
-                                                                order_slot_index(order_scratch, N));
+                                                                (uint32_t)total_leaf, keys_a, vals_a, grave);
     sort(sc.n_cur, key_bits, s);
     launch_head(skey, sc.n_cur, total_leaf, head, sc.n_alive, s);
     launch_worklist(head, total_leaf, work, d_work_count(), s);

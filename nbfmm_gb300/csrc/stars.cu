@@ -41,7 +41,7 @@ __global__ void import_kernel(StepCounters sc, const float2* __restrict__ cur, c
 __global__ void keys_from_state_kernel(Geometry g, StepCounters sc, const float4* __restrict__ state4,
                                        const float2* __restrict__ state_prev, uint32_t dead_key,
                                        uint32_t* __restrict__ keys, uint32_t* __restrict__ vals,
-                                       float4* __restrict__ grave, uint32_t* __restrict__ slot_index) {
+                                       float4* __restrict__ grave) {
   const int n = *sc.n_cur;
   const int prune = *sc.prune;
   const int death_rank = *sc.num_steps + 1 - (*sc.step - 1);  // later deaths first in the final order
@@ -56,7 +56,6 @@ __global__ void keys_from_state_kernel(Geometry g, StepCounters sc, const float4
     }
     keys[i] = key;
     vals[i] = (uint32_t)i;
-    slot_index[i] = (uint32_t)__float_as_int(p.w);
   }
 }
 
@@ -141,12 +140,12 @@ __device__ __forceinline__ OrderArrays order_arrays(uint32_t* base, int stride) 
 }
 
 // True when the cell's stars are not in index order (a descent between neighbours).
-__device__ __forceinline__ bool cell_out_of_order(const uint32_t* __restrict__ perm,
-                                                  const uint32_t* __restrict__ slot_index, int h0, int L, int lane) {
+__device__ __forceinline__ bool cell_out_of_order(const uint32_t* __restrict__ perm, const float4* __restrict__ state4,
+                                                  int h0, int L, int lane) {
   uint32_t last = 0u;
   for (int base = 0; base < L; base += 32) {
     const int i = base + lane;
-    const uint32_t o = i < L ? slot_index[perm[h0 + i]] : 0xffffffffu;
+    const uint32_t o = i < L ? (uint32_t)__float_as_int(state4[perm[h0 + i]].w) : 0xffffffffu;
     uint32_t before = __shfl_up_sync(0xffffffffu, o, 1);
     if (lane == 0) before = base == 0 ? 0u : last;
     if (__any_sync(0xffffffffu, i < L && i > 0 && before > o)) return true;
@@ -157,7 +156,7 @@ __device__ __forceinline__ bool cell_out_of_order(const uint32_t* __restrict__ p
 
 // Loads the cell's (index, slot) pairs and its increasing runs; returns the number of runs. Four chunks of 32 are
 // read per round (their slots, then their indices) to keep several loads in flight.
-__device__ int order_load(const uint32_t* __restrict__ perm, const uint32_t* __restrict__ slot_index, int h0, int L,
+__device__ int order_load(const uint32_t* __restrict__ perm, const float4* __restrict__ state4, int h0, int L,
                           const OrderArrays& a, int lane) {
   int runs = 0;
   uint32_t last = 0u;
@@ -171,7 +170,7 @@ __device__ int order_load(const uint32_t* __restrict__ perm, const uint32_t* __r
 #pragma unroll
     for (int u = 0; u < 4; ++u) {
       const int i = base + 32 * u + lane;
-      idx[u] = i < L ? slot_index[slot[u]] : 0xffffffffu;
+      idx[u] = i < L ? (uint32_t)__float_as_int(state4[slot[u]].w) : 0xffffffffu;
     }
 #pragma unroll
     for (int u = 0; u < 4; ++u) {
@@ -306,7 +305,6 @@ __global__ void __launch_bounds__(kStageWarps * 32, 4) gather_state_ordered_kern
     const float2* __restrict__ state_prev, float4* __restrict__ sorted4, float2* __restrict__ sprev,
     float4* __restrict__ cell0, uint32_t* __restrict__ scratch, int max_n) {
   __shared__ StageArrays stage[kStageWarps];
-  const uint32_t* __restrict__ slot_index = order_slot_index(scratch, max_n);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   StageArrays& st = stage[warp];
   const int warps = gridDim.x * kStageWarps;
@@ -470,9 +468,9 @@ __global__ void __launch_bounds__(kStageWarps * 32, 4) gather_state_ordered_kern
     }
     if (!done) {  // a cell larger than the stage, or of many runs
       const uint32_t* order = perm + h0;
-      if (L >= 2 && cell_out_of_order(perm, slot_index, h0, L, lane)) {
+      if (L >= 2 && cell_out_of_order(perm, state4, h0, L, lane)) {
         const OrderArrays a = order_arrays(scratch + h0, max_n);
-        order = order_merge(L, order_load(perm, slot_index, h0, L, a, lane), a, lane);
+        order = order_merge(L, order_load(perm, state4, h0, L, a, lane), a, lane);
       }
       for (int base = 0; base < L; base += 32) {
         const int i = base + lane;
@@ -508,10 +506,10 @@ void launch_import(const StepCounters& sc, const float2* cur, const float2* prev
 }
 
 void launch_keys_from_state(const Geometry& g, const StepCounters& sc, const float4* state4, const float2* state_prev,
-                            uint32_t dead_key, uint32_t* keys, uint32_t* vals, float4* grave, uint32_t* slot_index,
-                            int max_n, cudaStream_t stream) {
+                            uint32_t dead_key, uint32_t* keys, uint32_t* vals, float4* grave, int max_n,
+                            cudaStream_t stream) {
   keys_from_state_kernel<<<grid_for(max_n, 256, 152 * 16), 256, 0, stream>>>(g, sc, state4, state_prev, dead_key, keys,
-                                                                             vals, grave, slot_index);
+                                                                             vals, grave);
 }
 
 void launch_finish_step(const StepCounters& sc, cudaStream_t stream) { finish_step_kernel<<<1, 1, 0, stream>>>(sc); }

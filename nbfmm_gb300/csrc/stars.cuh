@@ -33,10 +33,9 @@ __device__ __forceinline__ int grave_fate(const float4* __restrict__ grave, int 
 void launch_set_int(int* p, int v, cudaStream_t stream);
 void launch_import(const StepCounters& sc, const float2* cur, const float2* prev, const float* w, float4* state4,
                    float2* state_prev, int max_n, cudaStream_t stream);
-// slot_index[i] receives the original index of state slot i (the order gather_state_ordered restores).
 void launch_keys_from_state(const Geometry& g, const StepCounters& sc, const float4* state4, const float2* state_prev,
-                            uint32_t dead_key, uint32_t* keys, uint32_t* vals, float4* grave, uint32_t* slot_index,
-                            int max_n, cudaStream_t stream);
+                            uint32_t dead_key, uint32_t* keys, uint32_t* vals, float4* grave, int max_n,
+                            cudaStream_t stream);
 void launch_finish_step(const StepCounters& sc, cudaStream_t stream);
 void launch_export_fate(const Geometry& g, const StepCounters& sc, const float4* state4, const float2* state_prev,
                         float4* grave, int max_n, cudaStream_t stream);
@@ -48,10 +47,8 @@ void launch_export_gather(const StepCounters& sc, const uint32_t* order, const f
 // The gather + P2M of a step over `num_cells` leaf cells of any layout (the batched form's global space too): the
 // state gathered into cell order with every leaf cell in index order, the order the reference's stable sort of the
 // caller's arrays gives (the step's sort keeps the previous cell order instead), and each cell's centre of mass
-// summed in that order. scratch holds kOrderScratch * max_n words: seven arrays for cells too large for shared
-// memory, then the original index of every state slot (order_slot_index), which the step's key pass writes.
-constexpr int kOrderScratch = 8;
-__host__ __device__ inline uint32_t* order_slot_index(uint32_t* scratch, int max_n) { return scratch + 7 * (size_t)max_n; }
+// summed in that order. scratch holds kOrderScratch * max_n words for cells too large for shared memory.
+constexpr int kOrderScratch = 7;
 void launch_gather_state_ordered(const int* head, int num_cells, const uint32_t* perm, const float4* state4,
                                  const float2* state_prev, float4* sorted4, float2* sprev, float4* cell0,
                                  uint32_t* scratch, int max_n, cudaStream_t stream);
