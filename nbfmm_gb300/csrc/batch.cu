@@ -402,7 +402,7 @@ struct nbfmm_batch {
     BATCH_TRY(balloc(&vals_b, N, "values"));
     BATCH_TRY(balloc(&counts, (size_t)(1 << kRadixMaxBits) * max_tiles, "tile counts"));
     BATCH_TRY(balloc(&digit_total, (size_t)(1 << kRadixMaxBits), "digit totals"));
-    BATCH_TRY(balloc(&work, (size_t)total_leaf + N / kP2PChunk + 1, "work list"));
+    BATCH_TRY(balloc(&work, work_list_capacity(total_leaf, N), "work list"));
     BATCH_TRY(balloc(&sorted4, N, "sorted particles"));
     BATCH_TRY(balloc(&sprev, N, "sorted previous positions"));
     BATCH_TRY(balloc(&cell4, (size_t)total_cells, "cells"));
@@ -495,7 +495,7 @@ struct nbfmm_batch {
                                                                 (uint32_t)total_leaf, keys_a, vals_a, grave);
     sort(sc.n_cur, key_bits, s);
     launch_head(skey, sc.n_cur, total_leaf, head, sc.n_alive, s);
-    launch_worklist(head, total_leaf, work, d_work_count(), s);
+    launch_worklist(head, total_leaf, work, d_work_count(), true, s);
     // gather + P2M over the global leaf space, each cell in index order
     launch_gather_state_ordered(head, total_leaf, perm, state4, state_prev, sorted4, sprev, cell4, order_scratch, N, s);
     for (int lv = 1; lv < max_levels; ++lv) {

@@ -28,6 +28,25 @@ constexpr int kP2PThreads = 128;        // 4 independent warps per CTA
 constexpr int kP2PPasses = 4;            // targets per lane in one work item (4 passes of 32)
 constexpr int kP2PChunk = 32 * kP2PPasses;  // targets per work item
 
+// Work list entries a solve may need: a non-empty cell of n targets yields at most n/kP2PChunk + 2 items
+// (its chunks and one paired-tail item) with paired tails, at most n/kP2PChunk + 1 without.
+inline size_t work_list_capacity(size_t num_cells, size_t n) { return 2 * num_cells + n / kP2PChunk + 1; }
+
+#ifndef NBFMM_P2P_PAIR_TAILS
+#define NBFMM_P2P_PAIR_TAILS 1  // 0: every cell's last partial pass stays in its own last chunk
+#endif
+
+#ifdef __CUDACC__
+// True when the last n mod 32 targets of leaf cell c and those of its row neighbour c ^ 1 run together in one
+// pass (cells 2i and 2i + 1 always share a row, in every system of a batch too): both cells have such a
+// partial pass and together they fill at most 32 lanes.
+__device__ __forceinline__ bool tails_paired(const int* __restrict__ head, int c) {
+  const int p = c ^ 1;
+  const int t = (head[c + 1] - head[c]) & 31, tp = (head[p + 1] - head[p]) & 31;
+  return NBFMM_P2P_PAIR_TAILS && t > 0 && tp > 0 && t + tp <= 32;
+}
+#endif
+
 struct Geometry {
   float xmin, ymin, xmax, ymax;  // position limits [x_min, y_min, x_max, y_max]
   float cell_x, cell_y;          // leaf cell size, (max - min) / B in FP32 (predo.cu:112-113)
@@ -157,7 +176,11 @@ void launch_head(const uint32_t* keys, const int* d_n, int num_cells, int* head,
                  cudaStream_t stream);
 
 // Work list of (cell, chunk) items over non-empty leaf cells; *d_work_count receives the count.
-void launch_worklist(const int* head, int num_cells, int2* work, int* d_work_count, cudaStream_t stream);
+// Work items of the non-empty cells: (cell, k) covers the cell's targets [128k, 128k + 128). With pair_tails
+// (the layout p2p_kernel reads), a cell whose tail is paired (tails_paired) clips its chunks to its whole passes
+// of 32 targets, and the even cell of the pair files one more item, (cell, -1): the tails of cell and cell + 1.
+void launch_worklist(const int* head, int num_cells, int2* work, int* d_work_count, bool pair_tails,
+                     cudaStream_t stream);
 
 // Gather the sorted particles from caller-order float2 positions and weights, and the leaf centres of
 // mass (P2M) of every leaf cell into level 0.

@@ -126,7 +126,7 @@ struct nbfmm_solver {
     NBFMM_TRY(dalloc(&counts, (size_t)(1 << kRadixMaxBits) * max_tiles, "tile counts"));
     NBFMM_TRY(dalloc(&digit_total, (size_t)(1 << kRadixMaxBits), "digit totals"));
     NBFMM_TRY(dalloc(&head, (size_t)num_cells + 2, "head"));
-    NBFMM_TRY(dalloc(&work, (size_t)num_cells + n / kP2PChunk + 1, "work list"));
+    NBFMM_TRY(dalloc(&work, work_list_capacity(num_cells, n), "work list"));
     NBFMM_TRY(dalloc(&sorted4, n, "sorted particles"));
     NBFMM_TRY(dalloc(&seff, n, "sorted effects"));
     NBFMM_TRY(dalloc(&cell4, (size_t)lv.total, "cells"));
@@ -158,13 +158,14 @@ struct nbfmm_solver {
     perm = where ? vals_b : vals_a;
   }
 
-  // Keys, sort, head and work list from caller-order positions (predo.cu:105-135 minus the gather).
-  void preassign(int n, const float2* pos, cudaStream_t s) {
+  // Keys, sort, head and work list from caller-order positions (predo.cu:105-135 minus the gather). The work
+  // list pairs tails (p2p_kernel's layout) unless the caller's kernel reads plain chunks.
+  void preassign(int n, const float2* pos, cudaStream_t s, bool pair_tails = true) {
     launch_set_int(d_n(), n, s);
     launch_keys_from_positions(geo, pos, d_n(), keys_a, vals_a, max_n, s);
     sort(d_n(), key_bits, s);
     launch_head(skey, d_n(), num_cells, head, d_n_alive(), s);
-    launch_worklist(head, num_cells, work, d_work_count(), s);
+    launch_worklist(head, num_cells, work, d_work_count(), pair_tails, s);
   }
 
   void far_field(cudaStream_t s) {

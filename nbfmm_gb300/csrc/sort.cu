@@ -187,17 +187,20 @@ __global__ void head_kernel(const uint32_t* __restrict__ keys, const int* __rest
 }
 
 __global__ void worklist_kernel(const int* __restrict__ head, int num_cells, int2* __restrict__ work,
-                                int* __restrict__ d_work_count) {
+                                int* __restrict__ d_work_count, int pair_tails) {
   const int lane = threadIdx.x & 31;
   // Whole warps iterate together so that the warp-wide scan below sees every lane.
   for (int base = blockIdx.x * blockDim.x; base < num_cells; base += gridDim.x * blockDim.x) {
     const int c = base + threadIdx.x;
-    int chunks = 0;
+    int chunks = 0, tails = 0;
     if (c < num_cells) {
       const int nt = head[c + 1] - head[c];
-      chunks = (nt + kP2PChunk - 1) / kP2PChunk;
+      const bool paired = pair_tails && tails_paired(head, c);
+      chunks = ((paired ? nt & ~31 : nt) + kP2PChunk - 1) / kP2PChunk;
+      tails = (paired && !(c & 1)) ? 1 : 0;  // the even cell files the pair
     }
-    int incl = chunks;
+    const int items = chunks + tails;
+    int incl = items;
 #pragma unroll
     for (int d = 1; d < 32; d <<= 1) {
       const int y = __shfl_up_sync(0xffffffffu, incl, d);
@@ -206,7 +209,9 @@ __global__ void worklist_kernel(const int* __restrict__ head, int num_cells, int
     int start = 0;
     if (lane == 31 && incl > 0) start = atomicAdd(d_work_count, incl);
     start = __shfl_sync(0xffffffffu, start, 31);
-    for (int k = 0; k < chunks; ++k) work[start + incl - chunks + k] = make_int2(c, k);
+    int2* out = work + start + incl - items;
+    for (int k = 0; k < chunks; ++k) out[k] = make_int2(c, k);
+    if (tails) out[chunks] = make_int2(c, -1);
   }
 }
 
@@ -264,9 +269,11 @@ void launch_head(const uint32_t* keys, const int* d_n, int num_cells, int* head,
   head_kernel<<<grid_for(num_cells + 1, 256, 152 * 16), 256, 0, stream>>>(keys, d_n, num_cells, head, d_n_alive);
 }
 
-void launch_worklist(const int* head, int num_cells, int2* work, int* d_work_count, cudaStream_t stream) {
+void launch_worklist(const int* head, int num_cells, int2* work, int* d_work_count, bool pair_tails,
+                     cudaStream_t stream) {
   cudaMemsetAsync(d_work_count, 0, sizeof(int), stream);
-  worklist_kernel<<<grid_for(num_cells, 256, 152 * 8), 256, 0, stream>>>(head, num_cells, work, d_work_count);
+  worklist_kernel<<<grid_for(num_cells, 256, 152 * 8), 256, 0, stream>>>(head, num_cells, work, d_work_count,
+                                                                        pair_tails ? 1 : 0);
 }
 
 void launch_keys_from_head(const int* head, int num_cells, uint32_t* skey, cudaStream_t stream) {
