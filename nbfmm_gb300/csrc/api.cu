@@ -251,6 +251,7 @@ struct nbfmm_stars {
   float2* state_prev = nullptr;
   float2* sprev = nullptr;
   float4* grave = nullptr;  // final states by original index: two float4 per star (stars.cuh file_grave)
+  float4* prune_rec = nullptr;  // prune()'s records, same layout
   uint32_t* order_scratch = nullptr;  // gather_state_ordered_kernel's scratch for large cells
   int* counters = nullptr;
   StepCounters sc{};
@@ -276,6 +277,7 @@ struct nbfmm_stars {
     NBFMM_TRY(dalloc(&state_prev, n, "state prev"));
     NBFMM_TRY(dalloc(&sprev, n, "sorted prev"));
     NBFMM_TRY(dalloc(&grave, 2 * n, "final states"));
+    NBFMM_TRY(dalloc(&prune_rec, 2 * n, "prune records"));
     NBFMM_TRY(dalloc(&order_scratch, kOrderScratch * n, "cell order scratch"));
     NBFMM_TRY(dalloc(&counters, 8, "step counters"));
     cudaMemset(cur, 0, n * sizeof(float2));
@@ -289,6 +291,7 @@ struct nbfmm_stars {
     sc.step = counters + 3;
     sc.prune = counters + 4;
     sc.num_steps = counters + 5;
+    sc.resume = counters + 6;  // two ints; 0: the first call imports
     launch_set_int(sc.num_star, num_star, nullptr);
     if (cudaStreamCreateWithFlags(&capture_stream, cudaStreamNonBlocking) != cudaSuccess ||
         cudaEventCreate(&cap_a) != cudaSuccess || cudaEventCreate(&cap_b) != cudaSuccess) {
@@ -319,7 +322,7 @@ struct nbfmm_stars {
     if (cap_b) cudaEventDestroy(cap_b);
     if (capture_stream) cudaStreamDestroy(capture_stream);
     dfree(cur); dfree(prev); dfree(w); dfree(state4); dfree(state_prev); dfree(sprev);
-    dfree(grave); dfree(order_scratch); dfree(counters);
+    dfree(grave); dfree(prune_rec); dfree(order_scratch); dfree(counters);
     delete solver;
   }
 
@@ -398,6 +401,7 @@ struct nbfmm_stars {
     if (steps <= 0) return NBFMM_OK;
     if (!step_graph) NBFMM_TRY(build_graph());
     nbfmm_solver& v = *solver;
+    launch_resume_check(sc, cur, prev, w, grave, max_n, s);
     launch_import(sc, cur, prev, w, state4, state_prev, max_n, s);
     launch_set_int(sc.num_steps, steps, s);
     for (int k = 0; k < steps; ++k) {
@@ -418,19 +422,20 @@ struct nbfmm_stars {
     launch_fate_keys(sc, grave, v.keys_a, v.vals_a, max_n, s);
     v.sort(sc.n_import, fate_bits(steps), s);
     launch_head(v.skey, sc.n_import, 1, v.head, sc.num_star, s);  // head[1] = number of fate-0 stars
-    launch_export_gather(sc, v.perm, grave, cur, prev, w, max_n, s);
+    launch_export_gather(sc, v.perm, grave, cur, prev, w, max_n, s, sc.resume);
     return cuda_check("nbfmm_stars_update");
   }
 
   // Stars::prune (prune.cu:28-62) on the public arrays: the one-bit stable sort of prune.cu:60, with the count
-  // of kept stars (prune.cu:61) left in the device counter. The final-state records serve as scratch: they
-  // are only live inside an update call.
+  // of kept stars (prune.cu:61) left in the device counter. It keeps its records apart from the final states
+  // of the last update call, which the next call compares the public arrays with; a prune that removes stars
+  // lowers num_star below that call's count, so the next call imports.
   void prune(cudaStream_t s) {
     nbfmm_solver& v = *solver;
-    launch_prune_keys(v.geo, sc, cur, prev, w, v.keys_a, v.vals_a, grave, max_n, s);
+    launch_prune_keys(v.geo, sc, cur, prev, w, v.keys_a, v.vals_a, prune_rec, max_n, s);
     v.sort(sc.n_import, 1, s);
     launch_head(v.skey, sc.n_import, 1, v.head, sc.num_star, s);  // head[1] = number of kept stars
-    launch_export_gather(sc, v.perm, grave, cur, prev, w, max_n, s);
+    launch_export_gather(sc, v.perm, prune_rec, cur, prev, w, max_n, s);
   }
 
   // Stars::display (display.cu:219-229): the frame of the current stars, then prune.
@@ -599,7 +604,7 @@ int nbfmm_stars_kernel_launches(nbfmm_stars* stars, int num_steps, long long* la
     return NBFMM_OK;
   }
   if (!stars->step_graph) NBFMM_TRY(stars->build_graph());
-  const int outside = 2 /* import, step count */ + 2 /* export fate, fate keys */ +
+  const int outside = 3 /* resume check, import, step count */ + 2 /* export fate, fate keys */ +
                       3 * stars->sort_passes(nbfmm_stars::fate_bits(num_steps)) + 1 /* head */ + 1 /* gather */;
   *launches = (long long)num_steps * stars->kernels_per_step + outside;
   return NBFMM_OK;

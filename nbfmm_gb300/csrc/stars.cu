@@ -25,7 +25,9 @@ __global__ void import_kernel(StepCounters sc, const float2* __restrict__ cur, c
                               const float* __restrict__ w, float4* __restrict__ state4,
                               float2* __restrict__ state_prev) {
   const int n = *sc.num_star;
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+  // Resuming, the state already holds these stars with these indices (in the last step's cell order).
+  const int copy = (sc.resume && sc.resume[0]) ? 0 : n;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < copy; i += gridDim.x * blockDim.x) {
     const float2 c = cur[i];
     state4[i] = make_float4(c.x, c.y, w[i], __int_as_float(i));
     state_prev[i] = prev[i];
@@ -36,6 +38,31 @@ __global__ void import_kernel(StepCounters sc, const float2* __restrict__ cur, c
     *sc.step = 1;
     *sc.prune = 0;
   }
+}
+
+// The state a call leaves is in the last step's cell order, and each call imports the public arrays afresh,
+// which puts the stars back in caller order and makes the first sort and gather of the call do full work. When
+// the previous call lost no star, its export was the identity (public entry i = record i), so public arrays
+// equal to the records bit for bit mean that the import would rebuild exactly the stars the state holds, with
+// the same original indices; the call then continues from the state. The step's result does not depend on the
+// order the state is in (the sort and the in-cell index order fix it), so both ways give the same bits.
+__global__ void resume_check_kernel(StepCounters sc, const float2* __restrict__ cur, const float2* __restrict__ prev,
+                                    const float* __restrict__ w, const float4* __restrict__ grave) {
+  const int n = *sc.num_star;
+  if (!sc.resume[0] || n != sc.resume[1]) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) sc.resume[0] = 0;
+    return;
+  }
+  bool same = true;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const float4 a = grave[2 * i];
+    const float m = grave[2 * i + 1].x;
+    const float2 c = cur[i], p = prev[i];
+    same &= __float_as_uint(c.x) == __float_as_uint(a.x) && __float_as_uint(c.y) == __float_as_uint(a.y) &&
+            __float_as_uint(p.x) == __float_as_uint(a.z) && __float_as_uint(p.y) == __float_as_uint(a.w) &&
+            __float_as_uint(w[i]) == __float_as_uint(m);
+  }
+  if (__any_sync(0xffffffffu, !same) && (threadIdx.x & 31) == 0) sc.resume[0] = 0;
 }
 
 __global__ void keys_from_state_kernel(Geometry g, StepCounters sc, const float4* __restrict__ state4,
@@ -87,8 +114,12 @@ __global__ void fate_keys_kernel(StepCounters sc, const float4* __restrict__ gra
 
 __global__ void export_gather_kernel(StepCounters sc, const uint32_t* __restrict__ order,
                                      const float4* __restrict__ grave, float2* __restrict__ cur,
-                                     float2* __restrict__ prev, float* __restrict__ w) {
+                                     float2* __restrict__ prev, float* __restrict__ w, int* __restrict__ mark) {
   const int n = *sc.n_import;
+  if (mark && blockIdx.x == 0 && threadIdx.x == 0) {
+    mark[0] = *sc.num_star == n ? 1 : 0;
+    mark[1] = *sc.num_star;
+  }
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     const uint32_t o = order[i];
     const float4 a = grave[2 * o];
@@ -525,8 +556,13 @@ void launch_fate_keys(const StepCounters& sc, const float4* grave, uint32_t* key
 }
 
 void launch_export_gather(const StepCounters& sc, const uint32_t* order, const float4* grave, float2* cur,
-                          float2* prev, float* w, int max_n, cudaStream_t stream) {
-  export_gather_kernel<<<grid_for(max_n, 256, 152 * 16), 256, 0, stream>>>(sc, order, grave, cur, prev, w);
+                          float2* prev, float* w, int max_n, cudaStream_t stream, int* mark) {
+  export_gather_kernel<<<grid_for(max_n, 256, 152 * 16), 256, 0, stream>>>(sc, order, grave, cur, prev, w, mark);
+}
+
+void launch_resume_check(const StepCounters& sc, const float2* cur, const float2* prev, const float* w,
+                         const float4* grave, int max_n, cudaStream_t stream) {
+  resume_check_kernel<<<grid_for(max_n, 256, 152 * 16), 256, 0, stream>>>(sc, cur, prev, w, grave);
 }
 
 void launch_gather_state_ordered(const int* head, int num_cells, const uint32_t* perm, const float4* state4,

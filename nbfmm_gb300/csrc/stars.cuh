@@ -14,6 +14,8 @@ struct StepCounters {
   int* step;       // 1-based step index within the call
   int* prune;      // 0 on the first step of a call (its input was pruned by the previous call)
   int* num_steps;  // steps of the current call
+  int* resume;     // Stars only: [0] 1 when the call may continue from the state the last update call left,
+                   // [1] the stars in that state (see launch_resume_check)
 };
 
 // The final state of a star filed under its original index ("grave"): a 32-byte record of two float4,
@@ -33,6 +35,11 @@ __device__ __forceinline__ int grave_fate(const float4* __restrict__ grave, int 
 void launch_set_int(int* p, int v, cudaStream_t stream);
 void launch_import(const StepCounters& sc, const float2* cur, const float2* prev, const float* w, float4* state4,
                    float2* state_prev, int max_n, cudaStream_t stream);
+// Clears sc.resume[0] unless the last update call lost no star, num_star is still the count it left
+// (sc.resume[1]), and the public arrays still hold, bit for bit, what it exported: its final states, filed in
+// `grave` by original index.
+void launch_resume_check(const StepCounters& sc, const float2* cur, const float2* prev, const float* w,
+                         const float4* grave, int max_n, cudaStream_t stream);
 void launch_keys_from_state(const Geometry& g, const StepCounters& sc, const float4* state4, const float2* state_prev,
                             uint32_t dead_key, uint32_t* keys, uint32_t* vals, float4* grave, int max_n,
                             cudaStream_t stream);
@@ -41,8 +48,11 @@ void launch_export_fate(const Geometry& g, const StepCounters& sc, const float4*
                         float4* grave, int max_n, cudaStream_t stream);
 void launch_fate_keys(const StepCounters& sc, const float4* grave, uint32_t* keys, uint32_t* vals, int max_n,
                       cudaStream_t stream);
+// Public arrays from the records: entry i = record order[i]. `mark`, if given (the end of an update call), gets
+// mark[0] = 1 if the call lost no star (then the export is the identity and the records describe the state)
+// and mark[1] = num_star.
 void launch_export_gather(const StepCounters& sc, const uint32_t* order, const float4* grave, float2* cur,
-                          float2* prev, float* w, int max_n, cudaStream_t stream);
+                          float2* prev, float* w, int max_n, cudaStream_t stream, int* mark = nullptr);
 
 // The gather + P2M of a step over `num_cells` leaf cells of any layout (the batched form's global space too): the
 // state gathered into cell order with every leaf cell in index order, the order the reference's stable sort of the

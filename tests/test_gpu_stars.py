@@ -118,11 +118,25 @@ def test_initialize_forwards_tick_and_state(engine):
     assert torch.all(torch.isfinite(st.gpuptr_position_cur_))
 
 
+def arrays(st):
+    n = st.num_star_
+    return (st.gpuptr_position_cur_[:n].cpu().numpy(), st.gpuptr_position_pre_[:n].cpu().numpy(),
+            st.gpuptr_weight_[:n].cpu().numpy())
+
+
+def assert_same_stars(a, b):
+    assert a.num_star_ == b.num_star_
+    for x, y in zip(arrays(a), arrays(b)):
+        np.testing.assert_array_equal(x.view(np.uint32), y.view(np.uint32))
+
+
 @pytest.mark.parametrize("level", [3, 5])
 def test_grouping_of_steps_into_calls_does_not_matter(engine, level):
-    """Stars crossing leaf cells at every step: K steps in one call equal K calls of one step, bit for bit. Each
-    call starts from the caller's order, so this holds only if every step orders each leaf cell by index, as the
-    reference's predo does (a stable sort of the caller's arrays), whatever cells the stars came from."""
+    """Stars crossing leaf cells at every step: K steps in one call equal K calls of one step, bit for bit, and
+    equal K fresh handles of one step each. A call continues from the state the last call left when the arrays
+    are unchanged; a fresh handle starts from the caller's order. Both agree only if every step orders each
+    leaf cell by index, as the reference's predo does (a stable sort of the caller's arrays), whatever cells
+    the stars came from."""
     import torch
 
     rng = np.random.default_rng(level)
@@ -136,8 +150,43 @@ def test_grouping_of_steps_into_calls_does_not_matter(engine, level):
     a.update(8)
     for _ in range(8):
         b.update(1)
+    c = make_stars(engine, cur, prev, w, level, lim, tick, eps)
+    for _ in range(8):
+        c.update(1)
+        c = make_stars(engine, *arrays(c), level, lim, tick, eps)
     torch.cuda.synchronize()
     assert a.num_star_ == b.num_star_
     assert torch.equal(a.gpuptr_position_cur_, b.gpuptr_position_cur_)
     assert torch.equal(a.gpuptr_position_pre_, b.gpuptr_position_pre_)
     assert torch.equal(a.gpuptr_weight_, b.gpuptr_weight_)
+    assert_same_stars(a, c)
+
+
+@pytest.mark.parametrize("case", ["edit", "loss", "prune", "edit_then_prune"])
+def test_a_call_resumes_only_from_its_own_export(engine, case):
+    """After an update call the engine keeps its state in cell order and continues from it when the public arrays
+    are bit for bit what the call exported and no star was lost. An edited star, a lost star (the last index,
+    whose loss leaves every other entry in place) and a prune in between must each give exactly the result of a
+    fresh handle on the same arrays."""
+    import torch
+
+    escape = [(2047, 0.2)] if case == "loss" else []
+    cur, prev, w = system(2048, 4, escape)
+    lim, tick, eps = (-1.0, -1.0, 1.0, 1.0), 1e-3, 1e-3
+    prev = (cur - (cur - prev) * 20).astype(np.float32)  # stars change cells between calls
+    if escape:
+        prev[2047] = [0.85 - 0.2, 0.0]
+    a = make_stars(engine, cur, prev, w, 3, lim, tick, eps)
+    a.update(3)
+    if case == "loss":
+        assert a.num_star_ == 2047
+    if case.startswith("edit"):
+        a.gpuptr_position_cur_[17, 0] += 1e-3
+    if case.endswith("prune"):
+        a.prune()
+        assert a.num_star_ == 2048
+    b = make_stars(engine, *arrays(a), 3, lim, tick, eps)
+    a.update(2)
+    b.update(2)
+    torch.cuda.synchronize()
+    assert_same_stars(a, b)
