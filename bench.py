@@ -24,11 +24,14 @@ if ROOT not in sys.path:
 
 FLOP_PER_PAIR = 15  # 2 sub, 3 for r^2, 1 sqrt, 1 for r*r^2 (+eps fused: 2), 1 rcp, 1 mul by m, 4 for 2 FMAs
 SMS, FP32_LANES, MUFU_LANES = 152, 128, 16
+# Transcendental-unit operations per pair in p2p_kernel's packed passes: the square root always, the hardware
+# reciprocal on the 10 of every 16 sources whose bit is clear in NBFMM_P2P_NEWTON_MASK = 0x9249 (p2p.cu).
+P2P_MUFU_PER_PAIR = 1 + 10 / 16
 WINDOW_CELLS = 32  # side of the CPU sample window, in leaf cells
 # DRAM bytes (read + write) of one P2P launch per particle, from the ncu capture of the two-disk workload at
-# N = 4,194,304 (profiles/p2p_kernel_two_disks.md: 131.65 MB + 73.63 MB); traffic grows with the particles
+# N = 4,194,304 (profiles/p2p_kernel_two_disks.md: 134.96 MB + 73.99 MB); traffic grows with the particles
 # of a launch (it equals the algorithmic 48 B/particle), so a full launch is this times N.
-P2P_DRAM_BYTES_PER_PARTICLE = (131.654144e6 + 73.634304e6) / 4194304
+P2P_DRAM_BYTES_PER_PARTICLE = (134.964992e6 + 73.988864e6) / 4194304
 
 
 def parse():
@@ -800,7 +803,8 @@ def main():
             "flop_per_pair": FLOP_PER_PAIR, "pairs_per_launch": pairs, "p2p_ms_per_launch": p2p_s * 1e3,
             "p2p_share_of_step": p2p_ms / max(elapsed_ms, 1e-9),
             "pairs_per_s": pairs / p2p_s,
-            "mufu_bound_pairs_per_s": SMS * MUFU_LANES * sm_mhz * 1e6 / 2,
+            "mufu_ops_per_pair": P2P_MUFU_PER_PAIR,
+            "mufu_bound_pairs_per_s": SMS * MUFU_LANES * sm_mhz * 1e6 / P2P_MUFU_PER_PAIR,
         },
         "e2e": {"value": replicas.whole_job_rate(n * e2e_steps, world, e2e_ms), "unit": "particle-steps/s",
                 "median_parts": e2e_parts, "clocks": e2e_clk,

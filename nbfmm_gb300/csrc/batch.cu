@@ -515,6 +515,7 @@ struct nbfmm_batch {
     a.sorted4 = sorted4;
     a.head = head;
     a.work = work;
+    a.pair_tails = 1;  // as a system stepped alone: pairing decides each pair's reciprocal method
     a.d_work_count = d_work_count();
     a.d_work_next = d_work_next();
     a.base_dim = 1;

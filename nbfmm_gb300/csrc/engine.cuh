@@ -33,7 +33,7 @@ constexpr int kP2PChunk = 32 * kP2PPasses;  // targets per work item
 inline size_t work_list_capacity(size_t num_cells, size_t n) { return 2 * num_cells + n / kP2PChunk + 1; }
 
 #ifndef NBFMM_P2P_PAIR_TAILS
-#define NBFMM_P2P_PAIR_TAILS 1  // 0: every cell's last partial pass stays in its own last chunk
+#define NBFMM_P2P_PAIR_TAILS 1  // 0: never pair tails, whatever a launch asks
 #endif
 
 #ifdef __CUDACC__
@@ -176,9 +176,13 @@ void launch_head(const uint32_t* keys, const int* d_n, int num_cells, int* head,
                  cudaStream_t stream);
 
 // Work list of (cell, chunk) items over non-empty leaf cells; *d_work_count receives the count.
-// Work items of the non-empty cells: (cell, k) covers the cell's targets [128k, 128k + 128). With pair_tails
-// (the layout p2p_kernel reads), a cell whose tail is paired (tails_paired) clips its chunks to its whole passes
-// of 32 targets, and the even cell of the pair files one more item, (cell, -1): the tails of cell and cell + 1.
+// Work items of the non-empty cells: (cell, k) covers the cell's targets [128k, 128k + 128). With pair_tails, a
+// cell whose tail is paired (tails_paired) clips its chunks to its whole passes of 32 targets, and the even
+// cell of the pair files one more item, (cell, -1): the tails of cell and cell + 1. p2p_kernel reads both
+// layouts (P2PArgs::pair_tails). Measured on GB300: pairing takes 1.4% off P2P on a 16.8M two-disk step and 5%
+// off 20k-star steps, and costs 5% on the batched form's launch of 512 small systems. The batched form pairs
+// all the same: which sources take the Newton reciprocal follows their place in a pass, so a batched system
+// stays bit-identical to the same system stepped alone only if both pair alike.
 void launch_worklist(const int* head, int num_cells, int2* work, int* d_work_count, bool pair_tails,
                      cudaStream_t stream);
 
@@ -215,6 +219,7 @@ struct P2PArgs {
   const float4* sorted4;   // sorted particles
   const int* head;         // leaf heads
   const int2* work;        // (cell, chunk) items
+  int pair_tails;          // the work list pairs tails (launch_worklist's pair_tails)
   const int* d_work_count;
   int* d_work_next;        // dynamic scheduling counter, zero before launch
   int base_dim;

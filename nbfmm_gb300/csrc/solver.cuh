@@ -179,6 +179,7 @@ struct nbfmm_solver {
     a.sorted4 = sorted4;
     a.head = head;
     a.work = work;
+    a.pair_tails = 1;  // every single-system work list here pairs tails
     a.d_work_count = d_work_count();
     a.d_work_next = d_work_next();
     a.base_dim = geo.base_dim;
