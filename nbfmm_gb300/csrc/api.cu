@@ -279,11 +279,11 @@ struct nbfmm_stars {
     NBFMM_TRY(dalloc(&grave, 2 * n, "final states"));
     NBFMM_TRY(dalloc(&prune_rec, 2 * n, "prune records"));
     NBFMM_TRY(dalloc(&order_scratch, kOrderScratch * n, "cell order scratch"));
-    NBFMM_TRY(dalloc(&counters, 8, "step counters"));
+    NBFMM_TRY(dalloc(&counters, 16, "step counters"));
     cudaMemset(cur, 0, n * sizeof(float2));
     cudaMemset(prev, 0, n * sizeof(float2));
     cudaMemset(w, 0, n * sizeof(float));
-    cudaMemset(counters, 0, 8 * sizeof(int));
+    cudaMemset(counters, 0, 16 * sizeof(int));
     sc.num_star = counters + 0;
     sc.n_import = counters + 1;
     sc.n_cur = counters + 2;
@@ -292,6 +292,7 @@ struct nbfmm_stars {
     sc.prune = counters + 4;
     sc.num_steps = counters + 5;
     sc.resume = counters + 6;  // two ints; 0: the first call imports
+    sc.sort_n = counters + 8;
     launch_set_int(sc.num_star, num_star, nullptr);
     if (cudaStreamCreateWithFlags(&capture_stream, cudaStreamNonBlocking) != cudaSuccess ||
         cudaEventCreate(&cap_a) != cudaSuccess || cudaEventCreate(&cap_b) != cudaSuccess) {
@@ -418,11 +419,13 @@ struct nbfmm_stars {
     }
     // Final prune and the reference's order: survivors (fate 0) in original order, then the pruned stars,
     // most recent first (fate 1, 2, ...), each group in original order.
+    // When the call lost no star (sort_n == 0) the fate keys, the sort and the head run over nothing and the
+    // export is the identity.
     launch_export_fate(v.geo, sc, state4, state_prev, grave, max_n, s);
     launch_fate_keys(sc, grave, v.keys_a, v.vals_a, max_n, s);
-    v.sort(sc.n_import, fate_bits(steps), s);
-    launch_head(v.skey, sc.n_import, 1, v.head, sc.num_star, s);  // head[1] = number of fate-0 stars
-    launch_export_gather(sc, v.perm, grave, cur, prev, w, max_n, s, sc.resume);
+    v.sort(sc.sort_n, fate_bits(steps), s);
+    launch_head(v.skey, sc.sort_n, 1, v.head, sc.num_star, s);  // head[1] = number of fate-0 stars
+    launch_export_gather(sc, v.perm, grave, cur, prev, w, max_n, s, sc.resume, sc.sort_n);
     return cuda_check("nbfmm_stars_update");
   }
 

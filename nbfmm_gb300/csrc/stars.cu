@@ -37,6 +37,7 @@ __global__ void import_kernel(StepCounters sc, const float2* __restrict__ cur, c
     *sc.n_import = n;
     *sc.step = 1;
     *sc.prune = 0;
+    if (sc.sort_n) *sc.sort_n = 0;  // raised by the export if the call loses a star
   }
 }
 
@@ -97,15 +98,20 @@ __global__ void finish_step_kernel(StepCounters sc) {
 __global__ void export_fate_kernel(Geometry g, StepCounters sc, const float4* __restrict__ state4,
                                    const float2* __restrict__ state_prev, float4* __restrict__ grave) {
   const int n = *sc.n_cur;
+  const int n0 = *sc.n_import;
+  // A star lost by a step or by this prune means the public order needs the fate sort.
+  if (sc.sort_n && blockIdx.x == 0 && threadIdx.x == 0 && n != n0) *sc.sort_n = n0;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     const float4 p = state4[i];
-    file_grave(grave, __float_as_int(p.w), p.x, p.y, state_prev[i], p.z, outside(g, p.x, p.y) ? 1 : 0);
+    const int fate = outside(g, p.x, p.y) ? 1 : 0;
+    file_grave(grave, __float_as_int(p.w), p.x, p.y, state_prev[i], p.z, fate);
+    if (fate && sc.sort_n) *sc.sort_n = n0;
   }
 }
 
 __global__ void fate_keys_kernel(StepCounters sc, const float4* __restrict__ grave, uint32_t* __restrict__ keys,
                                  uint32_t* __restrict__ vals) {
-  const int n = *sc.n_import;
+  const int n = sc.sort_n ? *sc.sort_n : *sc.n_import;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     keys[i] = (uint32_t)grave_fate(grave, i);
     vals[i] = (uint32_t)i;
@@ -114,14 +120,19 @@ __global__ void fate_keys_kernel(StepCounters sc, const float4* __restrict__ gra
 
 __global__ void export_gather_kernel(StepCounters sc, const uint32_t* __restrict__ order,
                                      const float4* __restrict__ grave, float2* __restrict__ cur,
-                                     float2* __restrict__ prev, float* __restrict__ w, int* __restrict__ mark) {
+                                     float2* __restrict__ prev, float* __restrict__ w, int* __restrict__ mark,
+                                     const int* __restrict__ sort_n) {
   const int n = *sc.n_import;
-  if (mark && blockIdx.x == 0 && threadIdx.x == 0) {
-    mark[0] = *sc.num_star == n ? 1 : 0;
-    mark[1] = *sc.num_star;
+  const bool identity = sort_n && *sort_n == 0;
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    if (identity) *sc.num_star = n;  // the fate sort and its head ran over nothing
+    if (mark) {
+      mark[0] = *sc.num_star == n ? 1 : 0;
+      mark[1] = *sc.num_star;
+    }
   }
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-    const uint32_t o = order[i];
+    const uint32_t o = identity ? (uint32_t)i : order[i];
     const float4 a = grave[2 * o];
     cur[i] = make_float2(a.x, a.y);
     prev[i] = make_float2(a.z, a.w);
@@ -556,8 +567,9 @@ void launch_fate_keys(const StepCounters& sc, const float4* grave, uint32_t* key
 }
 
 void launch_export_gather(const StepCounters& sc, const uint32_t* order, const float4* grave, float2* cur,
-                          float2* prev, float* w, int max_n, cudaStream_t stream, int* mark) {
-  export_gather_kernel<<<grid_for(max_n, 256, 152 * 16), 256, 0, stream>>>(sc, order, grave, cur, prev, w, mark);
+                          float2* prev, float* w, int max_n, cudaStream_t stream, int* mark, const int* sort_n) {
+  export_gather_kernel<<<grid_for(max_n, 256, 152 * 16), 256, 0, stream>>>(sc, order, grave, cur, prev, w, mark,
+                                                                           sort_n);
 }
 
 void launch_resume_check(const StepCounters& sc, const float2* cur, const float2* prev, const float* w,

@@ -16,6 +16,7 @@ struct StepCounters {
   int* num_steps;  // steps of the current call
   int* resume;     // Stars only: [0] 1 when the call may continue from the state the last update call left,
                    // [1] the stars in that state (see launch_resume_check)
+  int* sort_n;     // Stars only: entries the call's export sorts; 0 when it lost no star (identity export)
 };
 
 // The final state of a star filed under its original index ("grave"): a 32-byte record of two float4,
@@ -48,11 +49,13 @@ void launch_export_fate(const Geometry& g, const StepCounters& sc, const float4*
                         float4* grave, int max_n, cudaStream_t stream);
 void launch_fate_keys(const StepCounters& sc, const float4* grave, uint32_t* keys, uint32_t* vals, int max_n,
                       cudaStream_t stream);
-// Public arrays from the records: entry i = record order[i]. `mark`, if given (the end of an update call), gets
+// Public arrays from the records: entry i = record order[i], or record i where `sort_n` is given and holds 0
+// (nothing was sorted: then num_star = n_import). `mark`, if given (the end of an update call), gets
 // mark[0] = 1 if the call lost no star (then the export is the identity and the records describe the state)
 // and mark[1] = num_star.
 void launch_export_gather(const StepCounters& sc, const uint32_t* order, const float4* grave, float2* cur,
-                          float2* prev, float* w, int max_n, cudaStream_t stream, int* mark = nullptr);
+                          float2* prev, float* w, int max_n, cudaStream_t stream, int* mark = nullptr,
+                          const int* sort_n = nullptr);
 
 // The gather + P2M of a step over `num_cells` leaf cells of any layout (the batched form's global space too): the
 // state gathered into cell order with every leaf cell in index order, the order the reference's stable sort of the

@@ -190,3 +190,35 @@ def test_a_call_resumes_only_from_its_own_export(engine, case):
     b.update(2)
     torch.cuda.synchronize()
     assert_same_stars(a, b)
+
+
+def test_every_star_lost_and_an_empty_handle(engine, orc):
+    """Every star leaves the limits (at different steps); the arrays hold them in the reference's order, and
+    further calls on the now empty system (which cannot resume: the last call lost stars) step nothing. A handle
+    created with no stars updates, prunes and draws without error."""
+    import torch
+
+    n = 64
+    escape = [(i, 0.06 + 0.05 * (i % 4)) for i in range(n)]  # out after 3, 2, 1 and 1 steps
+    cur, prev, w = system(n, 5, escape)
+    lim, tick, eps = (-1.0, -1.0, 1.0, 1.0), 1e-3, 1e-3
+    st = make_stars(engine, cur, prev, w, 2, lim, tick, eps)
+    st.update(3)
+    torch.cuda.synchronize()
+    k, _, _, w_ref = oracle_steps(orc, cur, prev, w, 2, lim, tick, eps, 3)
+    assert st.num_star_ == k == 0
+    np.testing.assert_array_equal(st.gpuptr_weight_.cpu().numpy(), w_ref)
+    st.update(2)
+    st.prune()
+    torch.cuda.synchronize()
+    assert st.num_star_ == 0
+    np.testing.assert_array_equal(st.gpuptr_weight_.cpu().numpy(), w_ref)  # nothing moved
+
+    empty = engine.Stars(3, 0, 32, 24, 30, tick, 1.0, 0.01, lim, lim, epsilon=eps)
+    empty.update(4)
+    empty.prune()
+    board = torch.full((engine.frame_bytes(32, 24),), 7, dtype=torch.uint8, device="cuda")
+    empty.display(board)
+    torch.cuda.synchronize()
+    assert empty.num_star_ == 0
+    assert torch.all(board[:32 * 24] == 0) and torch.all(board[32 * 24:] == 128)
