@@ -225,6 +225,61 @@ def p2p_pairs(torch, head, base_dim):
     return int((n * (ns - 1)).clamp(min=0).sum().item())
 
 
+def stage_bandwidth(torch, solver, pos, w, n, num_level, reps=5):
+    """The solve's stages run one by one through the stage entry points (the reference's NBFMM_CHECK-public
+    methods) on `n` particles in caller order, each timed with CUDA events on the current stream (median of
+    `reps` after a warm-up), against its algorithmic bytes: HBM-bound sweeps reported in GB/s and as a fraction
+    of the measured copy bandwidth. P2P (compute-bound) is the step's roofline and is left out here."""
+    b = 1 << (num_level + 1)
+    c = b * b
+    levels = num_level if num_level > 0 else 1
+    dims = [b >> l for l in range(levels)]
+    passes = -(-2 * (num_level + 1) // 8)  # radix passes of at most 8 bits over the 2(L+1)-bit key
+    bytes_ = {
+        # keys (8 B read, 8 B written), each radix pass (4 B histogram read, 8 B read, 8 B written), the
+        # gather + leaf sums (permutation, position and weight read, sorted float4 written), heads and leaf cells
+        "predo": n * (16 + 20 * passes + 32) + c * 20,
+        "p2m": n * 16 + c * 20,
+        "m2m": sum((dims[l - 1] ** 2 + dims[l] ** 2) * 16 for l in range(1, levels)),
+        "m2l": sum(d * d * (16 + 8) for d in dims),
+        "l2l": sum(dims[l + 1] ** 2 * 8 + dims[l] ** 2 * 16 for l in range(levels - 1)),
+        "l2p": n * 20 + c * 8,
+        "postdo": n * 20,
+    }
+    eff = torch.empty(n, 2, device="cuda")
+    calls = {
+        "predo": lambda: solver.predo(n, pos, w), "p2m": lambda: solver.p2m(n), "m2m": solver.m2m,
+        "m2l": solver.m2l, "l2l": solver.l2l, "l2p": lambda: solver.l2p(n), "postdo": lambda: solver.postdo(n, eff),
+    }
+    solver.predo(n, pos, w)
+    solver.p2p(n)  # sorted effects for l2p / postdo
+    peak = measured_hbm_gbs()
+    out = {"workload": "one solve from caller order, stage by stage", "hbm_peak_gbs": peak}
+    for name, fn in calls.items():
+        fn()
+        times = []
+        for _ in range(reps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            fn()
+            e1.record()
+            e1.synchronize()
+            times.append(e0.elapsed_time(e1))
+        ms = statistics.median(times)
+        gbs = bytes_[name] / (ms / 1e3) / 1e9
+        out[name] = {"ms": ms, "bytes": bytes_[name], "gbs": gbs, "frac": gbs / peak if peak else None}
+    del eff
+    return out
+
+
+def measured_hbm_gbs():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["hbm_gbs"])
+    except (OSError, ValueError, KeyError):
+        return 6800.0  # fallback: one earlier STREAM-style copy on a GB300
+
+
 def fp64_error(torch, pos, w, eff, eps, targets):
     """Relative error of the engine's effects against the FP64 all-pairs direct sum, on the GPU, for targets."""
     p = pos.double()
@@ -677,6 +732,7 @@ def main():
     err64 = fp64_error(torch, pos, w, eff, sysm.epsilon, targets)
     del eff
     torch.cuda.empty_cache()  # return the FP64 check's temporaries
+    stages = stage_bandwidth(torch, solver, pos, w, n, sysm.num_level)
 
     stars = nbfmm_gb300.Stars(sysm.num_level, n, tick=sysm.dt, grav_const=sysm.grav_const,
                               position_limits=sysm.limits, epsilon=sysm.epsilon)
@@ -811,6 +867,7 @@ def main():
                 "h2d_bytes_per_step": io_bytes, "d2h_bytes_per_step": io_bytes,
                 "api": "Stars.update(1) per step, state copied in from and out to pinned host memory; the same "
                        "warm-up and timed steps as the device-timed value, from the same initial state"},
+        "stages": stages,
         "cpu_baseline": cpu,
         "gpu_launches": stars.kernel_launches(args.steps),
         "clocks": clk,
