@@ -92,19 +92,29 @@ __device__ __forceinline__ float2 kernel_exact(float2 t, float2 s, float m, floa
   return make_float2(__fmul_rn(dx, tmp), __fmul_rn(dy, tmp));
 }
 
-// Leaf sums of x*m, y*m and m over one cell, one warp per cell. Each lane contributes the products of one
-// particle of the current 32-particle chunk; the sums are then accumulated one particle at a time in sorted
-// order (lane 0, 1, ... of each chunk), so they round exactly like the sequential loop of the reference's
-// P2M check (check/core/solver/p2m.cu:36-46). Every lane ends with the same sums.
-__device__ __forceinline__ void cell_sums_add_chunk(float& sx, float& sy, float& sw, float x, float y, float m,
-                                                    int count) {
-  const float px = __fmul_rn(x, m);
-  const float py = __fmul_rn(y, m);
-  for (int j = 0; j < count; ++j) {
-    sx = __fadd_rn(sx, __shfl_sync(0xffffffffu, px, j));
-    sy = __fadd_rn(sy, __shfl_sync(0xffffffffu, py, j));
-    sw = __fadd_rn(sw, __shfl_sync(0xffffffffu, m, j));
+// The leaf sums of a cell (sum x*m, sum y*m, sum m), accumulated in sorted order one star at a time, so they
+// round exactly like the sequential loop of the reference's P2M check (check/core/solver/p2m.cu:36-46). A warp
+// adds one chunk of up to 32 consecutive stars (lane j holds star j): every lane puts its (x*m, y*m, m) into the
+// warp's buffer of 32 float4, then lane k < 3 adds component k of stars 0, 1, ... in turn into `acc`. That is one
+// shared-memory load and one add per star and component lane, where broadcasting each star to every lane took
+// three shuffles. Called by the whole warp with the same `count`; cell_sums_get reads the three sums.
+__device__ __forceinline__ void cell_sums_add_chunk(float& acc, float4* __restrict__ buf, float x, float y, float m,
+                                                    int count, int lane) {
+  buf[lane] = make_float4(__fmul_rn(x, m), __fmul_rn(y, m), m, 0.0f);
+  __syncwarp();
+  if (lane < 3) {
+    const float* b = reinterpret_cast<const float*>(buf) + lane;
+#pragma unroll 8
+    for (int j = 0; j < count; ++j) acc = __fadd_rn(acc, b[4 * j]);
   }
+  __syncwarp();  // the buffer is free for the next chunk
+}
+
+// The sums of cell_sums_add_chunk in every lane: (sum x*m, sum y*m, sum m).
+__device__ __forceinline__ void cell_sums_get(float acc, float& sx, float& sy, float& sw) {
+  sx = __shfl_sync(0xffffffffu, acc, 0);
+  sy = __shfl_sync(0xffffffffu, acc, 1);
+  sw = __shfl_sync(0xffffffffu, acc, 2);
 }
 
 // Centre of mass (p2m.cu:72): (sum x*m) / (sum m) per component; an empty cell is (0, 0) with mass 0.

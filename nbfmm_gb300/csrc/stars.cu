@@ -317,6 +317,7 @@ constexpr int kStageChunks = 10;                 // chunks of 32 stars held in r
 constexpr int kStageCap = 32 * kStageChunks;     // 320
 
 struct StageArrays {
+  float4 sums[32];  // cell_sums_add_chunk's buffer
   uint32_t key[kStageCap];
   float xs[kStageCap], ys[kStageCap], ms[kStageCap];
   int shift[kStageCap + 1];
@@ -352,7 +353,7 @@ __global__ void __launch_bounds__(kStageWarps * 32, 4) gather_state_ordered_kern
   const int warps = gridDim.x * kStageWarps;
   for (int c = blockIdx.x * kStageWarps + warp; c < num_cells; c += warps) {
     const int h0 = head[c], h1 = head[c + 1], L = h1 - h0;
-    float sx = 0.0f, sy = 0.0f, sw = 0.0f;
+    float acc = 0.0f;  // leaf sums, lanes 0-2
     bool done = false;
     if (L <= kStageCap) {
       uint32_t slot[kStageChunks], idx[kStageChunks];
@@ -405,7 +406,7 @@ __global__ void __launch_bounds__(kStageWarps * 32, 4) gather_state_ordered_kern
             sorted4[h0 + i] = q[u];
             sprev[h0 + i] = pv[u];
           }
-          cell_sums_add_chunk(sx, sy, sw, q[u].x, q[u].y, q[u].z, min(32, L - 32 * u));
+          cell_sums_add_chunk(acc, st.sums, q[u].x, q[u].y, q[u].z, min(32, L - 32 * u), lane);
         }
         done = true;
       } else {
@@ -501,8 +502,8 @@ __global__ void __launch_bounds__(kStageWarps * 32, 4) gather_state_ordered_kern
           for (int base = 0; base < L; base += 32) {
             const int j = base + lane;
             const bool in = j < L;
-            cell_sums_add_chunk(sx, sy, sw, in ? st.xs[j] : 0.0f, in ? st.ys[j] : 0.0f, in ? st.ms[j] : 0.0f,
-                                min(32, L - base));
+            cell_sums_add_chunk(acc, st.sums, in ? st.xs[j] : 0.0f, in ? st.ys[j] : 0.0f, in ? st.ms[j] : 0.0f,
+                                min(32, L - base), lane);
           }
           done = true;
         }
@@ -523,9 +524,11 @@ __global__ void __launch_bounds__(kStageWarps * 32, 4) gather_state_ordered_kern
           sorted4[h0 + i] = q;
           sprev[h0 + i] = state_prev[p];
         }
-        cell_sums_add_chunk(sx, sy, sw, q.x, q.y, q.z, min(32, L - base));
+        cell_sums_add_chunk(acc, st.sums, q.x, q.y, q.z, min(32, L - base), lane);
       }
     }
+    float sx, sy, sw;
+    cell_sums_get(acc, sx, sy, sw);
     if (lane == 0) cell0[c] = centre_of_mass(sx, sy, sw, h1 > h0);
     __syncwarp();  // the staging area is free for the next cell
   }
