@@ -343,7 +343,14 @@ __device__ __forceinline__ void warp_sort_pairs(uint32_t& k, int& v, int lane) {
   }
 }
 
-__global__ void __launch_bounds__(kStageWarps * 32, 4) gather_state_ordered_kernel(
+// Resident CTAs per SM the ordered gather is compiled and launched for (96 registers at 5, no spills). Measured
+// on the 16.8M two-disk step (100 steps, ms per step): 4 CTAs 16.385, 5 CTAs 16.362, 6 CTAs (80 registers,
+// spills) 16.409.
+#ifndef NBFMM_GATHER_MINB
+#define NBFMM_GATHER_MINB 5
+#endif
+
+__global__ void __launch_bounds__(kStageWarps * 32, NBFMM_GATHER_MINB) gather_state_ordered_kernel(
     int num_cells, const int* __restrict__ head, const uint32_t* __restrict__ perm, const float4* __restrict__ state4,
     const float2* __restrict__ state_prev, float4* __restrict__ sorted4, float2* __restrict__ sprev,
     float4* __restrict__ cell0, uint32_t* __restrict__ scratch, int max_n) {
@@ -583,7 +590,8 @@ void launch_resume_check(const StepCounters& sc, const float2* cur, const float2
 void launch_gather_state_ordered(const int* head, int num_cells, const uint32_t* perm, const float4* state4,
                                  const float2* state_prev, float4* sorted4, float2* sprev, float4* cell0,
                                  uint32_t* scratch, int max_n, cudaStream_t stream) {
-  gather_state_ordered_kernel<<<grid_for((long long)num_cells * 32, kStageWarps * 32, 152 * 4), kStageWarps * 32, 0,
+  gather_state_ordered_kernel<<<grid_for((long long)num_cells * 32, kStageWarps * 32, 152 * NBFMM_GATHER_MINB),
+                                kStageWarps * 32, 0,
                                 stream>>>(num_cells, head, perm, state4, state_prev, sorted4, sprev, cell0, scratch,
                                           max_n);
 }
