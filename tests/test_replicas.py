@@ -79,7 +79,8 @@ def test_two_gloo_ranks_run_independent_replicas(tmp_path, orc):
         np.testing.assert_array_equal(r["w"], w)
         assert float(r["slowest"]) == max(float(r0["elapsed"]), float(r1["elapsed"]))
         assert float(r["rate"]) == pytest.approx(2000 * 3 * 2 / (float(r["slowest"]) / 1e3))
-    assert float(r1["elapsed"]) > float(r0["elapsed"]) - 1.0
+    # each rank timed its own work, its sleep included (the ranks' compute times vary with the shared cores)
+    assert float(r0["elapsed"]) >= 50.0 and float(r1["elapsed"]) >= 100.0
 
 
 def test_one_rank_needs_no_process_group(monkeypatch):
