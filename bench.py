@@ -28,9 +28,10 @@ SMS, FP32_LANES, MUFU_LANES = 152, 128, 16
 # reciprocal on the 10 of every 16 sources whose bit is clear in NBFMM_P2P_NEWTON_MASK = 0x9249 (p2p.cu).
 P2P_MUFU_PER_PAIR = 1 + 10 / 16
 WINDOW_CELLS = 32  # side of the CPU sample window, in leaf cells
-# DRAM bytes (read + write) of one P2P launch per particle, from the ncu capture of the two-disk workload at
-# N = 4,194,304 (profiles/p2p_kernel_two_disks.md: 134.96 MB + 73.99 MB); traffic grows with the particles
-# of a launch (it equals the algorithmic 48 B/particle), so a full launch is this times N.
+# DRAM bytes (read + write) of one P2P launch per particle: ncu's dram__bytes_read.sum (134.96 MB) and
+# dram__bytes_write.sum (73.99 MB) for one p2p_kernel<kVerlet> launch of the two-disk step at N = 4,194,304,
+# depth 8 (the same particles per leaf cell as the 16.8M workload); traffic grows with the particles of a launch
+# (it equals the algorithmic 48 B/particle), so a full launch is this times N.
 P2P_DRAM_BYTES_PER_PARTICLE = (134.964992e6 + 73.988864e6) / 4194304
 
 
@@ -42,6 +43,8 @@ def parse():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--config", default="two_disks_16m")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--arithmetic", default="fast", choices=["fast", "exact"],
+                    help="near-field arithmetic of the engine (exact: correctly rounded, the oracle's rounding)")
     return ap.parse_args()
 
 
@@ -425,8 +428,8 @@ def run_adjoint(args):
     print(json.dumps(out), flush=True)
 
 
-# DRAM bytes (read + write) of one raster_bits_kernel launch per star, from the ncu capture of the display
-# workload itself (profiles/raster_kernel_two_disks.md: 201.60 MB + 3.42 MB at N = 16,777,216).
+# DRAM bytes (read + write) of one raster_bits_kernel launch per star: ncu's dram__bytes_read.sum (201.60 MB) and
+# dram__bytes_write.sum (3.42 MB) for one launch on the display workload itself (N = 16,777,216, 1920x1080).
 DISPLAY_DRAM_BYTES_PER_STAR = (201.596928e6 + 3.421184e6) / 16777216
 
 
@@ -721,7 +724,7 @@ def main():
     prev = torch.from_numpy(sysm.previous()).cuda()
 
     # One solve of the initial state: the P2P pair count and the error against the FP64 direct sum.
-    solver = nbfmm_gb300.Solver(sysm.num_level, n, sysm.limits, epsilon=sysm.epsilon)
+    solver = nbfmm_gb300.Solver(sysm.num_level, n, sysm.limits, epsilon=sysm.epsilon, arithmetic=args.arithmetic)
     eff = torch.empty(n, 2, device="cuda")
     solver.solve(n, pos, w, eff)
     torch.cuda.synchronize()
@@ -735,7 +738,7 @@ def main():
     stages = stage_bandwidth(torch, solver, pos, w, n, sysm.num_level)
 
     stars = nbfmm_gb300.Stars(sysm.num_level, n, tick=sysm.dt, grav_const=sysm.grav_const,
-                              position_limits=sysm.limits, epsilon=sysm.epsilon)
+                              position_limits=sysm.limits, epsilon=sysm.epsilon, arithmetic=args.arithmetic)
     stars.gpuptr_position_cur_.copy_(pos)
     stars.gpuptr_position_pre_.copy_(prev)
     stars.gpuptr_weight_.copy_(w)
@@ -771,7 +774,7 @@ def main():
     # pinned host memory, runs update(1) and copies the state out. ----
     e2e_steps = args.steps
     st2 = nbfmm_gb300.Stars(sysm.num_level, n, tick=sysm.dt, grav_const=sysm.grav_const,
-                            position_limits=sysm.limits, epsilon=sysm.epsilon)
+                            position_limits=sysm.limits, epsilon=sysm.epsilon, arithmetic=args.arithmetic)
     h_cur = torch.empty(n, 2, pin_memory=True)
     h_prev = torch.empty(n, 2, pin_memory=True)
     h_w = torch.empty(n, pin_memory=True)
@@ -844,7 +847,7 @@ def main():
         "dtype": "f32",
         "data": "synthetic (seeded; nbfmm_gb300/workloads.py)",
         "config": {"workload": workload_name(sysm), "N": n, "num_level": sysm.num_level,
-                   "steps_per_call": args.steps, "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
+                   "arithmetic": args.arithmetic, "steps_per_call": args.steps, "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
                    "l2": "inputs larger than L2 (state + sorted copy ~ 0.9 GB at N=16.8M)",
                    "stars_after_timed_steps": n_end},
         "roofline": {

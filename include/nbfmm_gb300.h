@@ -46,6 +46,17 @@ int nbfmm_solver_destroy(nbfmm_solver* solver);
  * (include/nbfmm/core/kernel_function.hpp:35), which is the default here. */
 int nbfmm_solver_set_epsilon(nbfmm_solver* solver, float epsilon);
 
+/* Arithmetic of the near field (P2P), per handle. No counterpart in the reference, whose kernelFunction
+ * (include/nbfmm/core/kernel_function.hpp:36-39) uses IEEE sqrt and division.
+ *   NBFMM_ARITH_FAST (default): hardware square-root and reciprocal approximations and fused multiply-adds, in
+ *     the reference's p2pNaive summation order; effects differ from IEEE evaluation in the last bits of each
+ *     pair, which cancellation can raise above 1e-5 relative on particles whose field nearly cancels.
+ *   NBFMM_ARITH_EXACT: every operation of kernelFunction's source rounded once, with correctly rounded sqrt and
+ *     division and no fused multiply-add, summed in p2pNaive order (p2p.cu:49-66): the effects round exactly
+ *     like the reference's algorithm evaluated in IEEE single precision. Slower near field. */
+enum { NBFMM_ARITH_FAST = 0, NBFMM_ARITH_EXACT = 1 };
+int nbfmm_solver_set_arithmetic(nbfmm_solver* solver, int arithmetic);
+
 /* nbfmm::Solver::solve(num_particle, position, weight, effect)  (solver.hpp:91-103, solve.cu:11-27).
  * Positions/weights in the caller's order in, effects in the caller's order out; 0 <= n <= max. */
 int nbfmm_solver_solve(nbfmm_solver* solver, int num_particle, const float* gpuptr_position_origin,
@@ -104,6 +115,9 @@ int nbfmm_stars_create(int fmm_level, int num_star, float tick, float grav_const
 int nbfmm_stars_destroy(nbfmm_stars* stars);
 int nbfmm_stars_set_epsilon(nbfmm_stars* stars, float epsilon);
 
+/* Near-field arithmetic of the update's solves (nbfmm_solver_set_arithmetic). */
+int nbfmm_stars_set_arithmetic(nbfmm_stars* stars, int arithmetic);
+
 /* The public state members (stars.hpp:60-72): gpuptr_position_cur_, gpuptr_position_pre_ (float2 [num_star]),
  * gpuptr_weight_ (float [num_star]). Stars::initialize (stars.hpp:111-114) is the caller writing these. */
 int nbfmm_stars_state(nbfmm_stars* stars, float** gpuptr_position_cur, float** gpuptr_position_pre,
@@ -131,6 +145,7 @@ int nbfmm_batch_create(int num_systems, const int* particle_offsets, const int* 
                        const float* position_limits, float tick, float grav_const, nbfmm_batch** out);
 int nbfmm_batch_destroy(nbfmm_batch* batch);
 int nbfmm_batch_set_epsilon(nbfmm_batch* batch, float epsilon);
+int nbfmm_batch_set_arithmetic(nbfmm_batch* batch, int arithmetic); /* nbfmm_solver_set_arithmetic */
 /* Device state arrays over all systems (float2 / float2 / float [particle_offsets[num_systems]]). */
 int nbfmm_batch_state(nbfmm_batch* batch, float** gpuptr_position_cur, float** gpuptr_position_pre,
                       float** gpuptr_weight);
@@ -245,8 +260,11 @@ int nbfmm_model_set_uniforms(const float* gpuptr_uniforms);
  * that cannot allocate device memory: a plugin whose host application owns every device buffer, or code
  * that must not trigger cudaMalloc's device synchronisation. It allocates nothing; its scratch is a fixed
  * device array inside the library (about 4.1 MB per GPU that loads it, held until exit), so at most 262,144
- * particles per call, and calls that overlap on the GPU race on that shared scratch. The first call on each
- * device looks up the scratch address (cudaGetSymbolAddress) and should come before any stream capture.
+ * particles per call, and calls that overlap on the GPU race on that shared scratch. Every call looks the
+ * scratch address up in the current CUDA context (cudaGetSymbolAddress, which neither allocates nor
+ * synchronises), so a context the host makes current, or a device reset, is followed; the first call on each
+ * device loads the library's module there and should come before any stream capture. A CUDA error pending
+ * from earlier work on the calling thread is reported (and cleared) before anything is launched.
  * Outputs: gpuptr_perm [num_particle] = original index of each sorted particle (the reference's
  * gpuptr_perm_), gpuptr_head [base_dim^2 + 1] = first sorted index of each leaf cell (gpuptr_head_). */
 int nbfmm_sort_cells_noalloc(int num_level, const float position_limits[4], int num_particle,

@@ -48,6 +48,8 @@ class Solver {
 
   // Engine extension: the kernel softening (the reference fixes 1e-1).
   void set_epsilon(float epsilon) { check(nbfmm_solver_set_epsilon(h_, epsilon)); }
+  // Engine extension: near-field arithmetic, NBFMM_ARITH_FAST (default) or NBFMM_ARITH_EXACT.
+  void set_arithmetic(int arithmetic) { check(nbfmm_solver_set_arithmetic(h_, arithmetic)); }
   nbfmm_solver* handle() { return h_; }
 
  private:

@@ -77,6 +77,15 @@ def _limits(position_limits):
     return (ctypes.c_float * 4)(*vals)
 
 
+ARITHMETIC = {"fast": _lib.NBFMM_ARITH_FAST, "exact": _lib.NBFMM_ARITH_EXACT}
+
+
+def _arithmetic(name: str) -> int:
+    if name not in ARITHMETIC:
+        raise ValueError(f"arithmetic must be one of {sorted(ARITHMETIC)}")
+    return ARITHMETIC[name]
+
+
 class _DeviceView:
     """Exposes a device range through __cuda_array_interface__ so torch can wrap it without a copy."""
 
@@ -94,7 +103,8 @@ def _as_tensor(ptr, shape, typestr):
 class Solver:
     """nbfmm::Solver (include/nbfmm/core/solver.hpp:22-209) on the GB300 engine."""
 
-    def __init__(self, num_level: int, max_num_particle: int, position_limits, epsilon: float = 0.1):
+    def __init__(self, num_level: int, max_num_particle: int, position_limits, epsilon: float = 0.1,
+                 arithmetic: str = "fast"):
         lib = _lib.load()
         h = ctypes.c_void_p()
         _check(lib.nbfmm_solver_create(int(num_level), int(max_num_particle), _limits(position_limits),
@@ -105,6 +115,7 @@ class Solver:
         self.max_num_particle = int(max_num_particle)
         self.position_limits = tuple(float(v) for v in position_limits)
         self.set_epsilon(epsilon)
+        self.set_arithmetic(arithmetic)
 
     def close(self):
         if getattr(self, "_h", None) is not None and self._h.value:
@@ -126,6 +137,12 @@ class Solver:
     def set_epsilon(self, epsilon: float):
         _check(_lib.load().nbfmm_solver_set_epsilon(self._h, float(epsilon)))
         self.epsilon = float(epsilon)
+
+    def set_arithmetic(self, arithmetic: str):
+        """Near-field arithmetic: "fast" (hardware approximations, the default) or "exact" (correctly rounded
+        sqrt and division, no fused multiply-add: the oracle's IEEE single-precision rounding)."""
+        _check(_lib.load().nbfmm_solver_set_arithmetic(self._h, _arithmetic(arithmetic)))
+        self.arithmetic = arithmetic
 
     def solve(self, num_particle, position, weight, effect, stream=None):
         """Solver::solve (solve.cu:11-27): effects of `num_particle` particles, caller order in and out."""
@@ -187,7 +204,7 @@ class Stars:
     """
 
     def __init__(self, fmm_level, num_star, width=1, height=1, fps=1, tick=None, grav_const=1.0, size_scale=1.0,
-                 position_limits=None, display_limits=None, *, epsilon: float = 0.1):
+                 position_limits=None, display_limits=None, *, epsilon: float = 0.1, arithmetic: str = "fast"):
         if tick is None or position_limits is None:
             raise ValueError("tick and position_limits are required")
         if int(width) <= 0 or int(height) <= 0 or int(fps) <= 0 or not float(size_scale) > 0:
@@ -211,6 +228,7 @@ class Stars:
         # tick_ = tick * sqrt(grav_const) in FP32 (stars.cu:31)
         self.tick_ = float(np.float32(tick) * np.sqrt(np.float32(grav_const)))
         self.set_epsilon(epsilon)
+        self.set_arithmetic(arithmetic)
         cur, pre, w = ctypes.c_void_p(), ctypes.c_void_p(), ctypes.c_void_p()
         _check(lib.nbfmm_stars_state(self._h, ctypes.byref(cur), ctypes.byref(pre), ctypes.byref(w)))
         self._ptrs = (cur.value, pre.value, w.value)
@@ -229,6 +247,11 @@ class Stars:
     def set_epsilon(self, epsilon: float):
         _check(_lib.load().nbfmm_stars_set_epsilon(self._h, float(epsilon)))
         self.epsilon = float(epsilon)
+
+    def set_arithmetic(self, arithmetic: str):
+        """Near-field arithmetic of the update's solves: "fast" (default) or "exact" (Solver.set_arithmetic)."""
+        _check(_lib.load().nbfmm_stars_set_arithmetic(self._h, _arithmetic(arithmetic)))
+        self.arithmetic = arithmetic
 
     @property
     def gpuptr_position_cur_(self):
@@ -292,7 +315,8 @@ class Batch:
     each system is one Stars::update of that system alone.
     """
 
-    def __init__(self, particle_offsets, num_levels, position_limits, tick, grav_const=1.0, epsilon: float = 0.1):
+    def __init__(self, particle_offsets, num_levels, position_limits, tick, grav_const=1.0, epsilon: float = 0.1,
+                 arithmetic: str = "fast"):
         import numpy as np
 
         off = np.ascontiguousarray(particle_offsets, dtype=np.int32)
@@ -311,6 +335,7 @@ class Batch:
         self.particle_offsets = off.tolist()
         self.num_particles = int(off[-1])
         self.set_epsilon(epsilon)
+        self.set_arithmetic(arithmetic)
         cur, pre, w = ctypes.c_void_p(), ctypes.c_void_p(), ctypes.c_void_p()
         _check(lib.nbfmm_batch_state(self._h, ctypes.byref(cur), ctypes.byref(pre), ctypes.byref(w)))
         self._ptrs = (cur.value, pre.value, w.value)
@@ -329,6 +354,11 @@ class Batch:
     def set_epsilon(self, epsilon: float):
         _check(_lib.load().nbfmm_batch_set_epsilon(self._h, float(epsilon)))
         self.epsilon = float(epsilon)
+
+    def set_arithmetic(self, arithmetic: str):
+        """Near-field arithmetic of every system's solves: "fast" (default) or "exact" (Solver.set_arithmetic)."""
+        _check(_lib.load().nbfmm_batch_set_arithmetic(self._h, _arithmetic(arithmetic)))
+        self.arithmetic = arithmetic
 
     @property
     def position_cur(self):

@@ -10,6 +10,8 @@ NBFMM_OK = 0
 NBFMM_ERR_INVALID = 1
 NBFMM_ERR_CUDA = 2
 NBFMM_ERR_NOMEM = 3
+NBFMM_ARITH_FAST = 0
+NBFMM_ARITH_EXACT = 1
 
 _c_int_p = ctypes.POINTER(ctypes.c_int)
 _c_float_p = ctypes.POINTER(ctypes.c_float)
@@ -22,6 +24,7 @@ SIGNATURES = {
     "nbfmm_solver_create": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, _c_float_p, ctypes.POINTER(_vp)]),
     "nbfmm_solver_destroy": (ctypes.c_int, [_vp]),
     "nbfmm_solver_set_epsilon": (ctypes.c_int, [_vp, ctypes.c_float]),
+    "nbfmm_solver_set_arithmetic": (ctypes.c_int, [_vp, ctypes.c_int]),
     "nbfmm_solver_solve": (ctypes.c_int, [_vp, ctypes.c_int, _vp, _vp, _vp, _vp]),
     "nbfmm_solver_predo": (ctypes.c_int, [_vp, ctypes.c_int, _vp, _vp, _vp]),
     "nbfmm_solver_p2p": (ctypes.c_int, [_vp, ctypes.c_int, _vp]),
@@ -36,6 +39,7 @@ SIGNATURES = {
                                           ctypes.POINTER(_vp)]),
     "nbfmm_stars_destroy": (ctypes.c_int, [_vp]),
     "nbfmm_stars_set_epsilon": (ctypes.c_int, [_vp, ctypes.c_float]),
+    "nbfmm_stars_set_arithmetic": (ctypes.c_int, [_vp, ctypes.c_int]),
     "nbfmm_stars_state": (ctypes.c_int, [_vp, ctypes.POINTER(_vp), ctypes.POINTER(_vp), ctypes.POINTER(_vp)]),
     "nbfmm_stars_num_star": (ctypes.c_int, [_vp, _c_int_p]),
     "nbfmm_stars_update": (ctypes.c_int, [_vp, ctypes.c_int, _vp]),
@@ -57,6 +61,7 @@ SIGNATURES = {
                                           ctypes.c_float, ctypes.POINTER(_vp)]),
     "nbfmm_batch_destroy": (ctypes.c_int, [_vp]),
     "nbfmm_batch_set_epsilon": (ctypes.c_int, [_vp, ctypes.c_float]),
+    "nbfmm_batch_set_arithmetic": (ctypes.c_int, [_vp, ctypes.c_int]),
     "nbfmm_batch_state": (ctypes.c_int, [_vp, ctypes.POINTER(_vp), ctypes.POINTER(_vp), ctypes.POINTER(_vp)]),
     "nbfmm_batch_num_stars": (ctypes.c_int, [_vp, _c_int_p]),
     "nbfmm_batch_update": (ctypes.c_int, [_vp, ctypes.c_int, _vp]),

@@ -125,6 +125,15 @@ int nbfmm_solver_set_epsilon(nbfmm_solver* solver, float epsilon) {
   return NBFMM_OK;
 }
 
+int nbfmm_solver_set_arithmetic(nbfmm_solver* solver, int arithmetic) {
+  NBFMM_TRY(check_solver(solver));
+  if (arithmetic != NBFMM_ARITH_FAST && arithmetic != NBFMM_ARITH_EXACT) {
+    return fail(NBFMM_ERR_INVALID, "arithmetic must be NBFMM_ARITH_FAST (0) or NBFMM_ARITH_EXACT (1)");
+  }
+  solver->exact = arithmetic;
+  return NBFMM_OK;
+}
+
 int nbfmm_solver_solve(nbfmm_solver* solver, int num_particle, const float* gpuptr_position_origin,
                        const float* gpuptr_weight_origin, float* gpuptr_effect_origin, void* stream) {
   NBFMM_TRY(check_solver(solver));
@@ -480,6 +489,13 @@ int nbfmm_stars_set_epsilon(nbfmm_stars* stars, float epsilon) {
   if (!stars) return fail(NBFMM_ERR_INVALID, "null stars handle");
   stars->drop_graph();  // the graph captured the old value
   return nbfmm_solver_set_epsilon(stars->solver, epsilon);
+}
+
+int nbfmm_stars_set_arithmetic(nbfmm_stars* stars, int arithmetic) {
+  if (!stars) return fail(NBFMM_ERR_INVALID, "null stars handle");
+  NBFMM_TRY(nbfmm_solver_set_arithmetic(stars->solver, arithmetic));
+  stars->drop_graph();  // the graph captured the old kernel
+  return NBFMM_OK;
 }
 
 int nbfmm_stars_state(nbfmm_stars* stars, float** gpuptr_position_cur, float** gpuptr_position_pre,

@@ -276,6 +276,7 @@ struct nbfmm_batch {
   int num_sms = 0;
   float tick = 0.0f;
   float eps = 0.1f;
+  int exact = 0;  // NBFMM_ARITH_EXACT
   std::vector<int> h_off, h_levels, h_dim, h_level_offset, h_level_total, h_tile_total;
 
   // Device tables.
@@ -520,6 +521,7 @@ struct nbfmm_batch {
     a.d_work_next = d_work_next();
     a.base_dim = 1;
     a.eps = eps;
+    a.exact = exact;
     a.ceff0 = ceff;  // level 0 = the global leaf space
     a.sprev = sprev;
     a.state4 = state4;
@@ -654,6 +656,16 @@ int nbfmm_batch_set_epsilon(nbfmm_batch* batch, float epsilon) {
   if (!(epsilon > 0.0f) || !std::isfinite(epsilon)) return api_fail(NBFMM_ERR_INVALID, "epsilon must be finite and > 0");
   batch->drop_graph();
   batch->eps = epsilon;
+  return NBFMM_OK;
+}
+
+int nbfmm_batch_set_arithmetic(nbfmm_batch* batch, int arithmetic) {
+  if (!batch) return api_fail(NBFMM_ERR_INVALID, "null batch handle");
+  if (arithmetic != NBFMM_ARITH_FAST && arithmetic != NBFMM_ARITH_EXACT) {
+    return api_fail(NBFMM_ERR_INVALID, "arithmetic must be NBFMM_ARITH_FAST (0) or NBFMM_ARITH_EXACT (1)");
+  }
+  batch->drop_graph();
+  batch->exact = arithmetic;
   return NBFMM_OK;
 }
 

@@ -234,6 +234,7 @@ struct P2PArgs {
   int* d_work_next;        // dynamic scheduling counter, zero before launch
   int base_dim;
   float eps;
+  int exact;               // 1: correctly rounded kernelFunction, no contraction (NBFMM_ARITH_EXACT)
   const float2* ceff0;     // level-0 local effects (kSolve, kVerlet), may be null when num_level == 0
   float2* seff;            // kStoreSorted: sorted effects
   float2* eff_origin;      // kSolve: effects in caller order

@@ -11,14 +11,15 @@
 // that loads the library until the process exits). Every call on a device uses the same array, which keeps
 // the last call's contents; nothing in it has to start at zero (each call writes every scratch word it
 // reads), but calls that overlap on the GPU -- on two streams, or from two host threads -- race on it.
-// The device address of the array is looked up with cudaGetSymbolAddress on the first call on each device
-// (that device current); that first call therefore does one runtime query and should come before any stream
-// capture.
+// The device address of the array belongs to one CUDA context: a context of its own that a host application
+// makes current, or the device's primary context after cudaDeviceReset, holds the array at another address.
+// So every call looks the address up in the current context with cudaGetSymbolAddress (a query that neither
+// allocates nor synchronises) instead of keeping one from an earlier call. The first call on a device also
+// loads the library's module there, so it should come before any stream capture.
 #include <cuda_runtime.h>
 
 #include <cmath>
 #include <cstdio>
-#include <mutex>
 #include <string>
 
 #include "../../include/nbfmm_gb300.h"
@@ -28,6 +29,12 @@
 namespace nbfmm_gb300 {
 int api_fail(int code, const char* fmt, ...);
 }
+
+#define NBFMM_TRY(expr)              \
+  do {                               \
+    const int _rc = (expr);          \
+    if (_rc != NBFMM_OK) return _rc; \
+  } while (0)
 
 namespace {
 
@@ -49,27 +56,15 @@ constexpr size_t kScratchWords = kCount + 64;  // the particle count, padded to 
 
 static __device__ __align__(256) uint32_t g_noalloc_scratch[kScratchWords];
 
-constexpr int kMaxDevices = 64;
-std::mutex g_setup_mutex;
-uint32_t* g_scratch_address[kMaxDevices] = {};
-
-// The device address of g_noalloc_scratch on the current device, looked up once per device.
+// The device address of g_noalloc_scratch in the current context, looked up on every call (see the file comment).
 int scratch_address(uint32_t** out) {
-  int dev = 0;
-  cudaError_t e = cudaGetDevice(&dev);
-  if (e != cudaSuccess) return api_fail(NBFMM_ERR_CUDA, "cudaGetDevice: %s", cudaGetErrorString(e));
-  if (dev < 0 || dev >= kMaxDevices) return api_fail(NBFMM_ERR_INVALID, "device ordinal %d not supported", dev);
-  std::lock_guard<std::mutex> lock(g_setup_mutex);
-  if (!g_scratch_address[dev]) {
-    void* p = nullptr;
-    e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-    if (e != cudaSuccess || !p) {
-      cudaGetLastError();
-      return api_fail(NBFMM_ERR_CUDA, "cudaGetSymbolAddress(scratch): %s", cudaGetErrorString(e));
-    }
-    g_scratch_address[dev] = static_cast<uint32_t*>(p);
+  void* p = nullptr;
+  const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+  if (e != cudaSuccess || !p) {
+    cudaGetLastError();
+    return api_fail(NBFMM_ERR_CUDA, "cudaGetSymbolAddress(scratch): %s", cudaGetErrorString(e));
   }
-  *out = g_scratch_address[dev];
+  *out = static_cast<uint32_t*>(p);
   return NBFMM_OK;
 }
 
@@ -94,9 +89,15 @@ extern "C" int nbfmm_sort_cells_noalloc(int num_level, const float position_limi
   if (!gpuptr_head || (num_particle > 0 && (!gpuptr_position || !gpuptr_perm))) {
     return api_fail(NBFMM_ERR_INVALID, "null device pointer");
   }
+  // An error left by the caller's earlier work is reported as such, not as this call's failure.
+  const cudaError_t pending = cudaGetLastError();
+  if (pending != cudaSuccess) {
+    return api_fail(NBFMM_ERR_CUDA, "nbfmm_sort_cells_noalloc: a CUDA error was pending before the call: %s",
+                    cudaGetErrorString(pending));
+  }
+  cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
   uint32_t* scratch = nullptr;
-  const int rc = scratch_address(&scratch);
-  if (rc != NBFMM_OK) return rc;
+  NBFMM_TRY(scratch_address(&scratch));
 
   const int B = 1 << (num_level + 1);
   Geometry g{};
@@ -108,7 +109,6 @@ extern "C" int nbfmm_sort_cells_noalloc(int num_level, const float position_limi
   g.cell_y = (l[3] - l[1]) / (float)B;
   g.num_level = num_level;
   g.base_dim = B;
-  cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
   int* d_n = reinterpret_cast<int*>(scratch + kCount);
   uint32_t* keys_a = scratch + kKeysA;
   uint32_t* vals_a = scratch + kValsA;
@@ -120,10 +120,11 @@ extern "C" int nbfmm_sort_cells_noalloc(int num_level, const float position_limi
   const uint32_t* skey = where ? scratch + kKeysB : keys_a;
   const uint32_t* perm = where ? scratch + kValsB : vals_a;
   launch_head(skey, d_n, B * B, gpuptr_head, nullptr, s);
-  if (num_particle > 0) {
-    cudaMemcpyAsync(gpuptr_perm, perm, (size_t)num_particle * sizeof(int), cudaMemcpyDeviceToDevice, s);
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess && num_particle > 0) {
+    e = cudaMemcpyAsync(gpuptr_perm, perm, (size_t)num_particle * sizeof(int), cudaMemcpyDeviceToDevice, s);
+    if (e != cudaSuccess) cudaGetLastError();
   }
-  const cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return api_fail(NBFMM_ERR_CUDA, "nbfmm_sort_cells_noalloc: %s", cudaGetErrorString(e));
   return NBFMM_OK;
 }

@@ -74,6 +74,7 @@ struct nbfmm_solver {
   int max_tiles = 0;
   int num_sms = 0;
   float eps = 0.1f;
+  int exact = 0;  // NBFMM_ARITH_EXACT: the near field with correctly rounded sqrt and division
 
   uint32_t *keys_a = nullptr, *vals_a = nullptr, *keys_b = nullptr, *vals_b = nullptr;
   uint32_t *counts = nullptr, *digit_total = nullptr;
@@ -184,6 +185,7 @@ struct nbfmm_solver {
     a.d_work_next = d_work_next();
     a.base_dim = geo.base_dim;
     a.eps = eps;
+    a.exact = exact;
     a.ceff0 = geo.num_level > 0 ? ceff0() : nullptr;
     return a;
   }

@@ -49,11 +49,12 @@ def run_alone(engine, cur, prev, w, level, lim, tick, eps, calls):
         st.gpuptr_weight_.cpu().numpy()
 
 
-def run_batch(engine, systems, tick, eps, calls):
+def run_batch(engine, systems, tick, eps, calls, arithmetic="fast"):
     import torch
 
     offsets = np.cumsum([0] + [len(s[2]) for s in systems])
-    b = engine.Batch(offsets, [s[3] for s in systems], [s[4] for s in systems], tick=tick, epsilon=eps)
+    b = engine.Batch(offsets, [s[3] for s in systems], [s[4] for s in systems], tick=tick, epsilon=eps,
+                     arithmetic=arithmetic)
     b.position_cur[:] = torch.from_numpy(np.concatenate([s[0] for s in systems])).cuda()
     b.position_pre[:] = torch.from_numpy(np.concatenate([s[1] for s in systems])).cuda()
     b.weight[:] = torch.from_numpy(np.concatenate([s[2] for s in systems])).cuda()
@@ -80,6 +81,28 @@ def test_batch_equals_systems_alone(engine, calls):
         np.testing.assert_array_equal(cur[sl], c)
         np.testing.assert_array_equal(pre[sl], p)
     assert sum(counts) < sum(len(s[2]) for s in systems)  # some stars were pruned
+
+
+def test_exact_arithmetic_batch_equals_the_oracle(engine, orc):
+    """With exact near-field arithmetic every system of a batch, stepped 3 times, equals the oracle's three
+    updates of that system alone bit for bit (positions, previous positions, weights, survivor counts)."""
+    systems = make_systems(9)
+    tick, eps = 2e-3, 1e-3
+    b, off = run_batch(engine, systems, tick, eps, [3], arithmetic="exact")
+    cur, pre, w = b.position_cur.cpu().numpy(), b.position_pre.cpu().numpy(), b.weight.cpu().numpy()
+    counts = b.num_stars
+    for s, (c0, p0, w0, level, lim) in enumerate(systems):
+        c, p, ww, n = c0.copy(), p0.copy(), w0.copy(), len(w0)
+        for _ in range(3):
+            if n == 0:
+                break
+            k, c[:n], p[:n], ww[:n], _ = orc.stars_update(c[:n], p[:n], ww[:n], level, lim, eps, np.float32(tick))
+            n = k
+        sl = slice(off[s], off[s + 1])
+        assert counts[s] == n, f"system {s}"
+        np.testing.assert_array_equal(w[sl], ww)
+        np.testing.assert_array_equal(cur[sl], c)
+        np.testing.assert_array_equal(pre[sl], p)
 
 
 def test_batch_launch_count_and_profile(engine):

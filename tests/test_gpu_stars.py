@@ -6,10 +6,11 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 
-def make_stars(engine, cur, prev, w, level, limits, tick, eps):
+def make_stars(engine, cur, prev, w, level, limits, tick, eps, arithmetic="fast"):
     import torch
 
-    st = engine.Stars(level, len(w), tick=tick, grav_const=1.0, position_limits=limits, epsilon=eps)
+    st = engine.Stars(level, len(w), tick=tick, grav_const=1.0, position_limits=limits, epsilon=eps,
+                      arithmetic=arithmetic)
     st.gpuptr_position_cur_[:] = torch.from_numpy(cur).cuda()
     st.gpuptr_position_pre_[:] = torch.from_numpy(prev).cuda()
     st.gpuptr_weight_[:] = torch.from_numpy(w).cuda()
@@ -76,6 +77,25 @@ def test_prune_order_over_several_updates(engine, orc):
     assert n < 2048 - 3
     assert st.num_star_ == n
     np.testing.assert_array_equal(st.gpuptr_weight_.cpu().numpy(), w_ref)  # identical layout
+
+
+@pytest.mark.parametrize("n,level,steps", [(2048, 3, 8), (60000, 5, 4)])
+def test_exact_arithmetic_updates_equal_the_oracle_bit_for_bit(engine, orc, n, level, steps):
+    """With exact near-field arithmetic, several updates (solve, Verlet, prune, stars escaping on the way) leave
+    the positions, previous positions, weights and star count exactly as the oracle's updates do."""
+    import torch
+
+    escape = [(5, 0.2), (17, 0.2), (300, 0.07), (1000, 0.07), (n - 1, 0.2)]
+    cur, prev, w = system(n, 40 + level, escape)
+    lim, tick, eps = (-1.0, -1.0, 1.0, 1.0), 1e-3, 1e-3
+    st = make_stars(engine, cur, prev, w, level, lim, tick, eps, arithmetic="exact")
+    st.update(steps)
+    torch.cuda.synchronize()
+    k, c_ref, p_ref, w_ref = oracle_steps(orc, cur, prev, w, level, lim, tick, eps, steps)
+    assert k < n and st.num_star_ == k
+    np.testing.assert_array_equal(st.gpuptr_weight_.cpu().numpy(), w_ref)
+    np.testing.assert_array_equal(st.gpuptr_position_pre_.cpu().numpy(), p_ref)
+    np.testing.assert_array_equal(st.gpuptr_position_cur_.cpu().numpy(), c_ref)
 
 
 def test_split_calls_equal_one_call(engine):
