@@ -38,11 +38,14 @@ P2P_DRAM_BYTES_PER_PARTICLE = (134.964992e6 + 73.988864e6) / 4194304
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--steps", type=int, default=None,
+                    help="timed steps (default: the workload's own step count; 200 for the frame modes)")
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--config", default="two_disks_16m")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="skip the side measurements of the default run (batched, adjoint, exact, CPU direct sums)")
     ap.add_argument("--arithmetic", default="fast", choices=["fast", "exact"],
                     help="near-field arithmetic of the engine (exact: correctly rounded, the oracle's rounding)")
     return ap.parse_args()
@@ -283,25 +286,87 @@ def measured_hbm_gbs():
         return 6800.0  # fallback: one earlier STREAM-style copy on a GB300
 
 
-def fp64_error(torch, pos, w, eff, eps, targets):
-    """Relative error of the engine's effects against the FP64 all-pairs direct sum, on the GPU, for targets."""
+def fp64_direct(torch, pos, w, eps, targets):
+    """FP64 all-pairs direct sum on the GPU for the listed targets (the error reference of every result)."""
     p = pos.double()
     m = w.double()
-    errs = []
+    out = []
     for t in targets.split(8):
         d = p[None, :, :] - p[t][:, None, :]  # (8, n, 2)
         r = torch.sqrt((d * d).sum(-1))
         s = m[None, :] / (r * r * r + eps)
         s[torch.arange(len(t), device=p.device), t] = 0.0
-        ref = (d * s[..., None]).sum(1)
-        errs.append(torch.linalg.norm(eff[t].double() - ref, dim=1) / torch.linalg.norm(ref, dim=1))
-    e = torch.cat(errs)
+        out.append((d * s[..., None]).sum(1))
+    return torch.cat(out)
+
+
+def rel_error_stats(torch, got, ref):
+    e = torch.linalg.norm(got.double() - ref, dim=1) / torch.linalg.norm(ref, dim=1)
     return {"median": float(e.median()), "p99": float(torch.quantile(e, 0.99)), "max": float(e.max()),
-            "targets": int(len(targets))}
+            "targets": int(len(ref))}
+
+
+def fp64_error(torch, pos, w, eff, eps, targets):
+    """Relative error of the engine's effects against the FP64 all-pairs direct sum, on the GPU, for targets."""
+    return rel_error_stats(torch, eff[targets], fp64_direct(torch, pos, w, eps, targets))
+
+
+def cpu_direct_baselines():
+    """OpenMP all-pairs direct sums on the host cores (the oracle library), FP32 (kernelFunction's operations)
+    and FP64, at N = 16,384 (every target) and N = 1,048,576 (2,048 sampled targets; the rate extrapolates to
+    a whole solve of N (N - 1) pairs)."""
+    from nbfmm_gb300 import workloads
+    from oracle import oracle
+
+    oracle.lib()
+    out = {"cores": oracle.num_threads(), "kind": "port",
+           "how": "orc_direct_f32 / orc_direct_f64, OpenMP over targets, all sources in index order"}
+    for name, sysm in (("plain_16k", workloads.plain(16384, 1, 3)), ("disk_1m", workloads.disk(1 << 20, 2, 6))):
+        n = sysm.n
+        targets = None if n <= 16384 else np.sort(np.random.default_rng(0).choice(n, 2048, replace=False))
+        nt = n if targets is None else len(targets)
+        for prec, fn in (("f32", oracle.direct_f32), ("f64", oracle.direct_f64)):
+            t0 = time.perf_counter()
+            fn(sysm.position, sysm.weight, sysm.epsilon, targets)
+            el = time.perf_counter() - t0
+            rate = nt * (n - 1) / el
+            solve_s = n * (n - 1) / rate
+            out[f"{name}_{prec}"] = {"pairs_per_s": rate, "solve_s": solve_s, "particle_steps_per_s": n / solve_s,
+                                     "targets_timed": nt}
+    return out
+
+
+def measure_exact(torch, nbfmm_gb300, sysm, pos, prev, w, steps, warmup):
+    """The same Stars steps with exact near-field arithmetic (correctly rounded sqrt and division, no
+    contraction: bit for bit the oracle's IEEE single-precision rounding)."""
+    st = nbfmm_gb300.Stars(sysm.num_level, sysm.n, tick=sysm.dt, grav_const=sysm.grav_const,
+                           position_limits=sysm.limits, epsilon=sysm.epsilon, arithmetic="exact")
+    st.gpuptr_position_cur_.copy_(pos)
+    st.gpuptr_position_pre_.copy_(prev)
+    st.gpuptr_weight_.copy_(w)
+    st.update(warmup)
+    torch.cuda.synchronize()
+    st.profile_begin(steps)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    st.update(steps)
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    p2p_ms, k = st.profile_end()
+    st.close()
+    return {"value": sysm.n * steps / (ms / 1e3), "unit": "particle-steps/s", "steps": steps, "warmup": warmup,
+            "ms_per_step": ms / steps, "p2p_ms_per_launch": p2p_ms / max(k, 1),
+            "what": "the same workload and Stars steps with Stars.set_arithmetic('exact')"}
 
 
 def run_batched(args):
     """The batched form against looped single-system updates on the same systems and depths."""
+    print(json.dumps(measure_batched(args.steps, args.warmup)), flush=True)
+
+
+def measure_batched(steps, warmup):
+    """The 512-system batched step against looped Stars updates of the same systems, depths and steps."""
     import torch
 
     import nbfmm_gb300
@@ -316,19 +381,19 @@ def run_batched(args):
     b.position_cur[:] = torch.from_numpy(sysb.position).cuda()
     b.position_pre[:] = torch.from_numpy(prev).cuda()
     b.weight[:] = torch.from_numpy(sysb.weight).cuda()
-    b.update(args.warmup)
+    b.update(warmup)
     torch.cuda.synchronize()
-    b.profile_begin(args.steps)
+    b.profile_begin(steps)
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     clocks = ClockSampler("0")
     e0.record()
-    b.update(args.steps)
+    b.update(steps)
     e1.record()
     torch.cuda.synchronize()
     clk = clocks.stop()
     batched_ms = e0.elapsed_time(e1)
     p2p_ms, p2p_k = b.profile_end()
-    launches = b.kernel_launches(args.steps)
+    launches = b.kernel_launches(steps)
     b.close()
 
     stars = []
@@ -339,34 +404,38 @@ def run_batched(args):
         st.gpuptr_position_cur_[:] = torch.from_numpy(sysb.position[lo:hi]).cuda()
         st.gpuptr_position_pre_[:] = torch.from_numpy(prev[lo:hi]).cuda()
         st.gpuptr_weight_[:] = torch.from_numpy(sysb.weight[lo:hi]).cuda()
-        st.update(args.warmup)
+        st.update(warmup)
         stars.append(st)
     torch.cuda.synchronize()
     e0.record()
     for st in stars:
-        st.update(args.steps)
+        st.update(steps)
     e1.record()
     torch.cuda.synchronize()
     looped_ms = e0.elapsed_time(e1)
-    value = n * args.steps / (batched_ms / 1e3)
-    looped = n * args.steps / (looped_ms / 1e3)
+    value = n * steps / (batched_ms / 1e3)
+    looped = n * steps / (looped_ms / 1e3)
     out = {
         "metric": "particle-steps/s", "value": value, "unit": "particle-steps/s", "n_gpus": 1,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": batched_ms / args.steps,
+        "steps": steps, "warmup": warmup, "ms_per_step": batched_ms / steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded; nbfmm_gb300/workloads.py batched)",
         "config": {"workload": f"batched: {sysb.num_systems} systems, N lognormal(median 20k, sd 0.8) clipped to "
                                f"[2k, 262k], {n:,} particles, squares and disks, eps {sysb.epsilon:g}, "
                                f"dt {sysb.dt:g}", "autotune": report},
-        "looped": {"value": looped, "ms_per_step": looped_ms / args.steps,
+        "looped": {"value": looped, "ms_per_step": looped_ms / steps,
                    "how": "one Stars per system with the same depths; update(K) per system, one after another"},
         "speedup_vs_looped": value / looped,
         "p2p_share_of_step": p2p_ms / batched_ms, "gpu_launches": launches, "clocks": clk,
     }
-    print(json.dumps(out), flush=True)
+    return out
 
 
 def run_adjoint(args):
+    print(json.dumps(measure_adjoint(args.steps, args.warmup)), flush=True)
+
+
+def measure_adjoint(steps, warmup):
     """Adjoint through the trajectory: forward pass and backward pass of the 262,144-particle disk (depth 6),
     dt 1e-4, checkpoints every 20 steps; targets = forward final positions + N(0, 1e-3)."""
     import torch
@@ -376,7 +445,6 @@ def run_adjoint(args):
     from nbfmm_gb300.adjoint import Adjoint
 
     sysm = workloads.disk(1 << 18, seed=5, num_level=5)
-    steps = args.steps
     n = sysm.n
     f = lambda a: torch.from_numpy(np.ascontiguousarray(a, np.float32)).cuda()
     x0, v0, m = f(sysm.position), f(sysm.velocity), f(sysm.weight)
@@ -388,7 +456,7 @@ def run_adjoint(args):
     g = torch.Generator(device="cpu").manual_seed(5)
     target = (xT.cpu() + 1e-3 * torch.randn(xT.shape, generator=g)).cuda()
     gx, gv, gm, terms = torch.empty_like(x0), torch.empty_like(v0), torch.empty_like(m), torch.empty_like(m)
-    for _ in range(max(1, args.warmup)):
+    for _ in range(max(1, warmup)):
         adj.forward(steps, x0, v0, m, xT)
         adj.backward(target, gx, gv, gm, terms)
     torch.cuda.synchronize()
@@ -417,7 +485,7 @@ def run_adjoint(args):
     stars_ms = e[0].elapsed_time(e[1])
     out = {
         "metric": "adjoint/forward time", "value": bwd / fwd, "unit": "ratio", "higher_is_better": False,
-        "n_gpus": 1, "steps": steps, "warmup": args.warmup, "dtype": "f32", "data": "synthetic (seeded disk)",
+        "n_gpus": 1, "steps": steps, "warmup": warmup, "dtype": "f32", "data": "synthetic (seeded disk)",
         "config": {"workload": f"adjoint: disk N={n:,}, depth 6, dt {sysm.dt:g}, eps {sysm.epsilon:g}, "
                                f"{steps} steps, checkpoint every 20, loss 0.5 sum m |x(T) - x*|^2"},
         "forward_ms_per_step": fwd / steps, "backward_ms_per_step": bwd / steps,
@@ -425,7 +493,7 @@ def run_adjoint(args):
         "stars_update_ms_per_step": stars_ms / steps, "backward_over_stars_step": bwd / stars_ms,
         "particle_steps_per_s_forward": n * steps / (fwd / 1e3), "clocks": clk,
     }
-    print(json.dumps(out), flush=True)
+    return out
 
 
 # DRAM bytes (read + write) of one raster_bits_kernel launch per star: ncu's dram__bytes_read.sum (201.60 MB) and
@@ -682,6 +750,14 @@ def main():
     args = parse()
     from nbfmm_gb300 import workloads
 
+    if args.steps is None:
+        own = {"batched_512": 100, "adjoint_262k": 200}
+        if args.config in own:
+            args.steps = own[args.config]
+        elif args.config in workloads.CONFIGS:
+            args.steps = workloads.CONFIGS[args.config]().steps
+        else:
+            args.steps = 200
     if args.config == "batched_512" and args.impl == "gb300":
         return run_batched(args)
     if args.config == "adjoint_262k" and args.impl == "gb300":
@@ -732,7 +808,18 @@ def main():
     pairs0 = p2p_pairs(torch, solver.buffers()["head"], b)
     g = torch.Generator(device="cpu").manual_seed(1234)
     targets = torch.randperm(n, generator=g)[:512].cuda()
-    err64 = fp64_error(torch, pos, w, eff, sysm.epsilon, targets)
+    ref64 = fp64_direct(torch, pos, w, sysm.epsilon, targets)
+    err64 = rel_error_stats(torch, eff[targets], ref64)
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        # the oracle's solve (the reference's algorithm in IEEE single precision) at the same targets
+        from oracle import oracle
+
+        t_sorted, order = torch.sort(targets)
+        ref_orc = oracle.solve_targets(sysm.position, sysm.weight, sysm.num_level, sysm.limits, sysm.epsilon,
+                                       t_sorted.cpu().numpy().astype(np.int32))
+        got_orc = torch.empty(len(targets), 2, dtype=torch.float32, device="cuda")
+        got_orc[order] = torch.from_numpy(ref_orc).cuda()
+        err64 = {"engine": err64, "oracle": rel_error_stats(torch, got_orc, ref64)}
     del eff
     torch.cuda.empty_cache()  # return the FP64 check's temporaries
     stages = stage_bandwidth(torch, solver, pos, w, n, sysm.num_level)
@@ -819,6 +906,17 @@ def main():
     del st2
     io_bytes = n * (8 + 8 + 4)
 
+    launches = stars.kernel_launches(args.steps)
+    extras = {}
+    if rank == 0 and world == 1 and not args.no_extras and args.config == "two_disks_16m":
+        extras["exact_arithmetic"] = measure_exact(torch, nbfmm_gb300, sysm, pos, prev, w, 10, 2)
+        del stars
+        torch.cuda.empty_cache()
+        extras["batched"] = measure_batched(100, 3)
+        extras["adjoint"] = measure_adjoint(200, 1)
+        if not args.no_cpu_baseline:
+            extras["cpu_direct"] = cpu_direct_baselines()
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         v, cores, ns, el = cpu_steps(sysm, 1000, budget_s=15.0)
@@ -872,10 +970,11 @@ def main():
                        "warm-up and timed steps as the device-timed value, from the same initial state"},
         "stages": stages,
         "cpu_baseline": cpu,
-        "gpu_launches": stars.kernel_launches(args.steps),
+        "gpu_launches": launches,
         "clocks": clk,
         "error_vs_fp64": err64,
     }
+    out.update(extras)
     print(json.dumps(out), flush=True)
     replicas.finish(dist)
 

@@ -469,6 +469,28 @@ void orc_direct_f64(int n, const float* pos, const float* w, double eps, const i
   }
 }
 
+/* FP32 all-pairs direct sum (demo.cu:59-66 pattern), each pair evaluated as kernelFunction does, sources in
+ * index order: the CPU direct-sum baseline of the benchmark. */
+void orc_direct_f32(int n, const float* pos, const float* w, float eps, const int* targets, int n_targets,
+                    float* eff) {
+  const int nt = targets ? n_targets : n;
+#pragma omp parallel for schedule(dynamic, 16)
+  for (int t = 0; t < nt; ++t) {
+    const int i = targets ? targets[t] : t;
+    const float tx = pos[2 * i], ty = pos[2 * i + 1];
+    float ex = 0.0f, ey = 0.0f;
+    for (int j = 0; j < n; ++j) {
+      if (j == i) continue;
+      float ax, ay;
+      orc_kernel_function(tx, ty, pos[2 * j], pos[2 * j + 1], w[j], eps, &ax, &ay);
+      ex += ax;
+      ey += ay;
+    }
+    eff[2 * t] = ex;
+    eff[2 * t + 1] = ey;
+  }
+}
+
 long long orc_p2p_pairs(int base_dim, const int* head) {
   const int B = base_dim;
   long long total = 0;

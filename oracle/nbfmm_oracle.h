@@ -92,6 +92,10 @@ int orc_stars_update(int n, int num_level, const float limits[4], float eps, int
 /* FP64 all-pairs direct sum (demo.cu:59-66 pattern) for the listed targets (all when targets == NULL). */
 void orc_direct_f64(int n, const float* pos, const float* w, double eps, const int* targets, int n_targets,
                     double* eff);
+/* The same all-pairs direct sum in FP32 with kernelFunction's operations (kernel_function.hpp:36-39), sources in
+ * index order: the CPU direct-sum baseline of the benchmark. */
+void orc_direct_f32(int n, const float* pos, const float* w, float eps, const int* targets, int n_targets,
+                    float* eff);
 
 /* Number of P2P pairs of a sorted system (targets x sources over each 3x3 block, self excluded). */
 long long orc_p2p_pairs(int base_dim, const int* head);

@@ -52,6 +52,7 @@ def lib():
             "orc_display_threads": (None, [c_int, c_int, c_int, c_float, _f, _f, _f, _u8]),
             "orc_stars_update": (c_int, [c_int, c_int, _f, c_float, c_int, c_float, _f, _f, _f, _f]),
             "orc_direct_f64": (None, [c_int, _f, _f, ctypes.c_double, ctypes.c_void_p, c_int, _d]),
+            "orc_direct_f32": (None, [c_int, _f, _f, ctypes.c_float, ctypes.c_void_p, c_int, _f]),
             "orc_p2p_pairs": (ctypes.c_longlong, [c_int, _i]),
             "orc_num_threads": (c_int, []),
             "orc_model_circle": (None, [c_int] + [c_float] * 6 + [c_int, _f, _f, _f, _f]),
@@ -185,6 +186,19 @@ def direct_f64(pos, w, eps, targets=None):
     else:
         t = i32(targets)
         lib().orc_direct_f64(n, f32(pos), f32(w), float(eps), t.ctypes.data_as(ctypes.c_void_p), nt, eff)
+    return eff
+
+
+def direct_f32(pos, w, eps, targets=None):
+    """All-pairs direct sum in FP32 (kernelFunction's operations, sources in index order)."""
+    n = len(w)
+    nt = n if targets is None else len(targets)
+    eff = np.zeros((nt, 2), np.float32)
+    if targets is None:
+        lib().orc_direct_f32(n, f32(pos), f32(w), float(eps), None, 0, eff)
+    else:
+        t = i32(targets)
+        lib().orc_direct_f32(n, f32(pos), f32(w), float(eps), t.ctypes.data_as(ctypes.c_void_p), nt, eff)
     return eff
 
 
