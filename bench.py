@@ -240,11 +240,16 @@ def stage_bandwidth(torch, solver, pos, w, n, num_level, reps=5):
     c = b * b
     levels = num_level if num_level > 0 else 1
     dims = [b >> l for l in range(levels)]
-    passes = -(-2 * (num_level + 1) // 8)  # radix passes of at most 8 bits over the 2(L+1)-bit key
+    key_bits = 2 * (num_level + 1)
+    passes = 1 if key_bits <= 10 else -(-key_bits // 10)  # record-sort passes of at most 10 bits
+    # Record sort: the first pass reads positions twice (keys for the tile counts, then for ranking: 8 B each)
+    # and weights once (4 B), and writes key + record (20 B); each later pass reads keys twice (4 B each) and
+    # the record (16 B) and writes key + record (20 B); the last pass also writes the permutation (4 B). Then
+    # heads (4 B per cell, binary searches in cache), the work list and the leaf sums (16 B read per particle,
+    # 16 B written per leaf cell).
+    sort_bytes = 40 + 44 * (passes - 1) + 4
     bytes_ = {
-        # keys (8 B read, 8 B written), each radix pass (4 B histogram read, 8 B read, 8 B written), the
-        # gather + leaf sums (permutation, position and weight read, sorted float4 written), heads and leaf cells
-        "predo": n * (16 + 20 * passes + 32) + c * 20,
+        "predo": n * (sort_bytes + 16) + c * 28,
         "p2m": n * 16 + c * 20,
         "m2m": sum((dims[l - 1] ** 2 + dims[l] ** 2) * 16 for l in range(1, levels)),
         "m2l": sum(d * d * (16 + 8) for d in dims),
@@ -274,6 +279,10 @@ def stage_bandwidth(torch, solver, pos, w, n, num_level, reps=5):
         ms = statistics.median(times)
         gbs = bytes_[name] / (ms / 1e3) / 1e9
         out[name] = {"ms": ms, "bytes": bytes_[name], "gbs": gbs, "frac": gbs / peak if peak else None}
+        if name == "predo":
+            # the task's own minimum (read x, y, m; write the sorted x, y, m and the permutation; heads)
+            task = n * 28 + (c + 1) * 4
+            out[name].update(task_bytes=task, task_frac=task / (ms / 1e3) / 1e9 / peak if peak else None)
     del eff
     return out
 

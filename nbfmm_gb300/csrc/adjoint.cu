@@ -525,8 +525,7 @@ struct nbfmm_adjoint {
   // VJP of one solve at positions `pos` (original order) for effect adjoint scale * lam; results in gx, gm.
   void vjp(const float2* pos, const float2* lam, float scale, cudaStream_t s) {
     nbfmm_solver& v = *solver;
-    v.preassign(n, pos, s, false);  // adj_p2p_kernel reads plain 128-target chunks
-    launch_gather_p2m(v.geo, v.head, v.perm, pos, m, v.sorted4, v.cell0(), s);
+    v.predo(n, pos, m, s, false);  // adj_p2p_kernel reads plain 128-target chunks
     const int cells = v.num_cells;
     adj_gather_kernel<<<grid_for((long long)cells * 32, 256, 152 * 16), 256, 0, s>>>(cells, v.head, v.perm, lam,
                                                                                     scale, smu, cell_lam);

@@ -152,10 +152,8 @@ int nbfmm_solver_predo(nbfmm_solver* solver, int num_particle, const float* gpup
   if (num_particle > 0 && (!gpuptr_position_origin || !gpuptr_weight_origin)) {
     return fail(NBFMM_ERR_INVALID, "null device pointer");
   }
-  cudaStream_t s = as_stream(stream);
-  solver->preassign(num_particle, reinterpret_cast<const float2*>(gpuptr_position_origin), s);
-  launch_gather_p2m(solver->geo, solver->head, solver->perm, reinterpret_cast<const float2*>(gpuptr_position_origin),
-                    gpuptr_weight_origin, solver->sorted4, solver->cell0(), s);
+  solver->predo(num_particle, reinterpret_cast<const float2*>(gpuptr_position_origin), gpuptr_weight_origin,
+                as_stream(stream));
   return cuda_check("nbfmm_solver_predo");
 }
 

@@ -23,7 +23,8 @@ constexpr int kMaxLevels = 11;           // num_level in [0, 10], B <= 2048
 constexpr int kSortThreads = 256;        // radix sort CTA
 constexpr int kSortItems = 16;           // items per thread
 constexpr int kSortTile = kSortThreads * kSortItems;  // 4096 items per tile
-constexpr int kRadixMaxBits = 8;
+constexpr int kRadixMaxBits = 10;        // digit bits per pass of the (key, value) radix sort: 2 passes for 20 bits
+constexpr int kRecMaxBits = 10;          // digit bits per pass of the record sort (launch_sort_records)
 constexpr int kP2PThreads = 128;        // 4 independent warps per CTA
 constexpr int kP2PPasses = 4;            // targets per lane in one work item (4 passes of 32)
 constexpr int kP2PChunk = 32 * kP2PPasses;  // targets per work item
@@ -181,6 +182,15 @@ int launch_radix_sort(uint32_t* keys_a, uint32_t* vals_a, uint32_t* keys_b, uint
                       uint32_t* counts, uint32_t* digit_total, const int* d_n, int max_n, int key_bits,
                       cudaStream_t stream);
 
+// Stable LSD radix sort of caller-order particles by leaf key, carrying each particle's record: on return
+// rec_final[i] = (x, y, m, original index bits), key_final[i] its leaf key and perm[i] its original index, in
+// key order (ties in caller order). rec_tmp / key_tmp hold the passes in between. counts needs
+// 2^kRecMaxBits * ceil(max_n / kSortTile) words and digit_total 2^kRecMaxBits.
+int record_sort_passes(int key_bits);
+void launch_sort_records(const Geometry& g, const float2* pos, const float* w, const int* d_n, int max_n,
+                         int key_bits, float4* rec_final, float4* rec_tmp, uint32_t* key_final, uint32_t* key_tmp,
+                         uint32_t* perm, uint32_t* counts, uint32_t* digit_total, cudaStream_t stream);
+
 // head[c] = first index with key >= c, c in [0, num_cells]; *d_n_alive = head[num_cells].
 void launch_head(const uint32_t* keys, const int* d_n, int num_cells, int* head, int* d_n_alive,
                  cudaStream_t stream);
@@ -196,12 +206,7 @@ void launch_head(const uint32_t* keys, const int* d_n, int num_cells, int* head,
 void launch_worklist(const int* head, int num_cells, int2* work, int* d_work_count, bool pair_tails,
                      cudaStream_t stream);
 
-// Gather the sorted particles from caller-order float2 positions and weights, and the leaf centres of
-// mass (P2M) of every leaf cell into level 0.
-void launch_gather_p2m(const Geometry& g, const int* head, const uint32_t* perm, const float2* pos,
-                       const float* w, float4* sorted4, float4* cell0, cudaStream_t stream);
-
-// P2M alone on already sorted particles (stage entry point).
+// P2M on the sorted particles: leaf centres of mass summed in sorted order (predo, and the stage entry point).
 void launch_p2m(const Geometry& g, const int* head, const float4* sorted4, float4* cell0, cudaStream_t stream);
 
 // M2M, every level 1..L-1.

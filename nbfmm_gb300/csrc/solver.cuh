@@ -81,6 +81,7 @@ struct nbfmm_solver {
   int* head = nullptr;
   int2* work = nullptr;
   float4* sorted4 = nullptr;
+  float4* rec_tmp = nullptr;  // the record sort's passes in between
   float2* seff = nullptr;
   float4* cell4 = nullptr;
   float2* ceff = nullptr;
@@ -124,11 +125,13 @@ struct nbfmm_solver {
     NBFMM_TRY(dalloc(&vals_a, n, "values"));
     NBFMM_TRY(dalloc(&keys_b, n, "keys"));
     NBFMM_TRY(dalloc(&vals_b, n, "values"));
-    NBFMM_TRY(dalloc(&counts, (size_t)(1 << kRadixMaxBits) * max_tiles, "tile counts"));
-    NBFMM_TRY(dalloc(&digit_total, (size_t)(1 << kRadixMaxBits), "digit totals"));
+    constexpr int kDigits = 1 << (kRecMaxBits > kRadixMaxBits ? kRecMaxBits : kRadixMaxBits);
+    NBFMM_TRY(dalloc(&counts, (size_t)kDigits * max_tiles, "tile counts"));
+    NBFMM_TRY(dalloc(&digit_total, (size_t)kDigits, "digit totals"));
     NBFMM_TRY(dalloc(&head, (size_t)num_cells + 2, "head"));
     NBFMM_TRY(dalloc(&work, work_list_capacity(num_cells, n), "work list"));
     NBFMM_TRY(dalloc(&sorted4, n, "sorted particles"));
+    NBFMM_TRY(dalloc(&rec_tmp, n, "sort records"));
     NBFMM_TRY(dalloc(&seff, n, "sorted effects"));
     NBFMM_TRY(dalloc(&cell4, (size_t)lv.total, "cells"));
     NBFMM_TRY(dalloc(&ceff, (size_t)lv.total, "cell effects"));
@@ -146,7 +149,7 @@ struct nbfmm_solver {
   ~nbfmm_solver() {
     dfree(keys_a); dfree(vals_a); dfree(keys_b); dfree(vals_b);
     dfree(counts); dfree(digit_total); dfree(head); dfree(work);
-    dfree(sorted4); dfree(seff); dfree(cell4); dfree(ceff); dfree(ints);
+    dfree(sorted4); dfree(rec_tmp); dfree(seff); dfree(cell4); dfree(ceff); dfree(ints);
   }
 
   float4* cell0() { return cell4 + lv.offset[0]; }
@@ -159,14 +162,18 @@ struct nbfmm_solver {
     perm = where ? vals_b : vals_a;
   }
 
-  // Keys, sort, head and work list from caller-order positions (predo.cu:105-135 minus the gather). The work
-  // list pairs tails (p2p_kernel's layout) unless the caller's kernel reads plain chunks.
-  void preassign(int n, const float2* pos, cudaStream_t s, bool pair_tails = true) {
+  // predo.cu:105-135 plus P2M's leaf sums: caller-order positions and weights sorted by leaf cell as records
+  // (sorted4 = x, y, m, original index; skey, perm), heads, the P2P work list (paired tails unless the caller's
+  // kernel reads plain chunks) and the leaf centres of mass, summed in sorted order.
+  void predo(int n, const float2* pos, const float* w, cudaStream_t s, bool pair_tails = true) {
     launch_set_int(d_n(), n, s);
-    launch_keys_from_positions(geo, pos, d_n(), keys_a, vals_a, max_n, s);
-    sort(d_n(), key_bits, s);
+    launch_sort_records(geo, pos, w, d_n(), max_n, 2 * (geo.num_level + 1), sorted4, rec_tmp, keys_a, keys_b,
+                        vals_a, counts, digit_total, s);
+    skey = keys_a;
+    perm = vals_a;
     launch_head(skey, d_n(), num_cells, head, d_n_alive(), s);
     launch_worklist(head, num_cells, work, d_work_count(), pair_tails, s);
+    launch_p2m(geo, head, sorted4, cell0(), s);
   }
 
   void far_field(cudaStream_t s) {
@@ -192,8 +199,7 @@ struct nbfmm_solver {
 
   int solve(int n, const float* pos, const float* w, float* eff, cudaStream_t s) {
     if (n == 0) return NBFMM_OK;
-    preassign(n, reinterpret_cast<const float2*>(pos), s);
-    launch_gather_p2m(geo, head, perm, reinterpret_cast<const float2*>(pos), w, sorted4, cell0(), s);
+    predo(n, reinterpret_cast<const float2*>(pos), w, s);
     far_field(s);
     P2PArgs a = p2p_args();
     a.eff_origin = reinterpret_cast<float2*>(eff);

@@ -7,9 +7,9 @@
 // equals the order of the integer key iy*B + ix, and cub's merge sort keeps equal keys in input order, so a
 // stable radix sort on that key reproduces the reference's permutation bit for bit.
 //
-// Sort design: per pass, an upsweep writes each 4096-item tile's digit histogram, one CTA per digit scans
-// its row of tile counts, and a downsweep ranks each tile's items stably (warp match + per-warp digit
-// counters in shared memory) and scatters them. Every kernel reads the element count from device memory,
+// Sort design: per pass (digits of up to 10 bits), an upsweep writes each 4096-item tile's digit histogram, one
+// CTA per digit scans its row of tile counts, and a downsweep ranks each tile's items stably (warp match +
+// per-warp digit counters in shared memory) and scatters them. Every kernel reads the element count from device memory,
 // so the same launches serve any n <= max_n without a host round trip (and can be captured in a graph).
 #include "engine.cuh"
 
@@ -45,6 +45,19 @@ __device__ __forceinline__ uint32_t block_exclusive_scan_256(uint32_t v, uint32_
   *total = warp_sums[kSortThreads / 32 - 1];
   __syncthreads();
   return warp_prefix + x - v;
+}
+
+// Exclusive scan of up to kSortThreads * 4 values v[tid*4 .. tid*4+3] over a 256-thread block.
+__device__ __forceinline__ void block_exclusive_scan_4x256(uint32_t* v4, uint32_t* warp_sums) {
+  const uint32_t local = v4[0] + v4[1] + v4[2] + v4[3];
+  uint32_t total;
+  uint32_t run = block_exclusive_scan_256(local, warp_sums, &total);
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    const uint32_t c = v4[k];
+    v4[k] = run;
+    run += c;
+  }
 }
 
 __global__ void keys_from_positions_kernel(Geometry g, const float2* __restrict__ pos, const int* __restrict__ d_n,
@@ -120,26 +133,38 @@ radix_downsweep_kernel(const uint32_t* __restrict__ keys_in, const uint32_t* __r
   const int lane = threadIdx.x & 31;
   const int warp = threadIdx.x >> 5;
 
-  // Start of every digit in the output: exclusive scan of the digit totals.
+  // Start of every digit in the output: exclusive scan of the digit totals (4 digits per thread).
   {
-    const uint32_t v = (threadIdx.x < nd) ? digit_total[threadIdx.x] : 0u;
-    uint32_t total;
-    const uint32_t ex = block_exclusive_scan_256(v, warp_sums, &total);
-    if (threadIdx.x < nd) digit_base[threadIdx.x] = ex;
+    uint32_t v[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const int d = threadIdx.x * 4 + k;
+      v[k] = d < nd ? digit_total[d] : 0u;
+    }
+    block_exclusive_scan_4x256(v, warp_sums);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const int d = threadIdx.x * 4 + k;
+      if (d < nd) digit_base[d] = v[k];
+    }
   }
   for (int d = lane; d < nd; d += 32) warp_hist[warp][d] = 0u;
   __syncwarp();
 
-  // Warp `warp` owns items [warp*512, warp*512 + 512) of the tile, in 16 rounds of 32 consecutive items.
+  // Warp `warp` owns items [warp*512, warp*512 + 512) of the tile, in 16 rounds of 32 consecutive items. The
+  // keys are all loaded before the ranking (16 loads per thread in flight); values are read when scattered.
   const int base = t * kSortTile + warp * (32 * kSortItems);
   const unsigned lt_mask = (1u << lane) - 1u;
-  uint32_t key[kSortItems], val[kSortItems], rank[kSortItems];
+  uint32_t key[kSortItems], rank[kSortItems];
+#pragma unroll
+  for (int r = 0; r < kSortItems; ++r) {
+    const int i = base + r * 32 + lane;
+    key[r] = i < n ? keys_in[i] : 0u;
+  }
 #pragma unroll
   for (int r = 0; r < kSortItems; ++r) {
     const int i = base + r * 32 + lane;
     const bool valid = i < n;
-    key[r] = valid ? keys_in[i] : 0u;
-    val[r] = valid ? vals_in[i] : 0u;
     const uint32_t digit = valid ? ((key[r] >> shift) & mask) : (uint32_t)nd;  // nd marks an empty slot
     const unsigned peers = __match_any_sync(0xffffffffu, digit);
     const uint32_t before = valid ? warp_hist[warp][digit] : 0u;
@@ -167,7 +192,140 @@ radix_downsweep_kernel(const uint32_t* __restrict__ keys_in, const uint32_t* __r
       const uint32_t digit = (key[r] >> shift) & mask;
       const uint32_t dst = warp_hist[warp][digit] + rank[r];
       keys_out[dst] = key[r];
-      vals_out[dst] = val[r];
+      vals_out[dst] = vals_in[i];
+    }
+  }
+}
+
+// ---- Record sort: the solve's predo ----------------------------------------------------------------------
+//
+// The keys are computed from the caller-order positions inside the passes (never stored in caller order), and
+// each particle's record (x, y, m, original index) travels with its key through the passes, so the sorted
+// particles come out of the last pass and no gather through the permutation (a random 32-byte sector per 8- or
+// 4-byte read) follows. Digits of up to kRecMaxBits bits: two passes for the keys of depth <= 10 leaf grids.
+// Per pass: an upsweep of per-tile digit counts, the per-digit scan, and a downsweep that loads the tile's
+// items into registers first, ranks them stably (the warp-match ranking of radix_downsweep_kernel) and
+// scatters key and record.
+
+template <bool FROM_POS>
+__global__ void __launch_bounds__(kSortThreads)
+rec_upsweep_kernel(Geometry g, const float2* __restrict__ pos, const uint32_t* __restrict__ keys,
+                   const int* __restrict__ d_n, int shift, int bits, uint32_t* __restrict__ counts, int max_tiles) {
+  __shared__ uint32_t hist[1 << kRecMaxBits];
+  const int n = *d_n;
+  const int t = blockIdx.x;
+  if (t >= num_tiles(n)) return;
+  const int nd = 1 << bits;
+  const uint32_t mask = (uint32_t)nd - 1u;
+  for (int d = threadIdx.x; d < nd; d += kSortThreads) hist[d] = 0u;
+  __syncthreads();
+  const int base = t * kSortTile;
+  const int end = min(base + kSortTile, n);
+  for (int i = base + threadIdx.x; i < end; i += kSortThreads) {
+    uint32_t key;
+    if (FROM_POS) {
+      const float2 p = pos[i];
+      key = leaf_key(g, p.x, p.y);
+    } else {
+      key = keys[i];
+    }
+    atomicAdd(&hist[(key >> shift) & mask], 1u);
+  }
+  __syncthreads();
+  for (int d = threadIdx.x; d < nd; d += kSortThreads) counts[(size_t)d * max_tiles + t] = hist[d];
+}
+
+template <bool FROM_POS, bool FINAL>
+__global__ void __launch_bounds__(kSortThreads, 2)
+rec_downsweep_kernel(Geometry g, const float2* __restrict__ pos, const float* __restrict__ w,
+                     const uint32_t* __restrict__ keys_in, const float4* __restrict__ rec_in,
+                     uint32_t* __restrict__ keys_out, float4* __restrict__ rec_out, uint32_t* __restrict__ perm_out,
+                     const int* __restrict__ d_n, int shift, int bits, const uint32_t* __restrict__ counts,
+                     const uint32_t* __restrict__ digit_total, int max_tiles) {
+  constexpr int kWarps = kSortThreads / 32;
+  __shared__ uint32_t warp_hist[kWarps][1 << kRecMaxBits];
+  __shared__ uint32_t digit_base[1 << kRecMaxBits];
+  __shared__ uint32_t warp_sums[kWarps];
+  const int n = *d_n;
+  const int t = blockIdx.x;
+  if (t >= num_tiles(n)) return;
+  const int nd = 1 << bits;
+  const uint32_t mask = (uint32_t)nd - 1u;
+  const int lane = threadIdx.x & 31;
+  const int warp = threadIdx.x >> 5;
+
+  // The tile's keys (the first pass computes them from the positions and keeps x, y), loaded before any
+  // ranking so that all 16 loads per thread are in flight together; the rest of each record is read when it
+  // is scattered.
+  const int base = t * kSortTile + warp * (32 * kSortItems);
+  uint32_t key[kSortItems];
+  float px[FROM_POS ? kSortItems : 1], py[FROM_POS ? kSortItems : 1];
+#pragma unroll
+  for (int r = 0; r < kSortItems; ++r) {
+    const int i = base + r * 32 + lane;
+    if (FROM_POS) {
+      const float2 p = (i < n) ? pos[i] : make_float2(0.0f, 0.0f);
+      px[r] = p.x;
+      py[r] = p.y;
+      key[r] = leaf_key(g, p.x, p.y);
+    } else {
+      key[r] = (i < n) ? keys_in[i] : 0u;
+    }
+  }
+
+  // Start of every digit in the output: exclusive scan of the digit totals (4 digits per thread).
+  {
+    uint32_t v[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const int d = threadIdx.x * 4 + k;
+      v[k] = d < nd ? digit_total[d] : 0u;
+    }
+    block_exclusive_scan_4x256(v, warp_sums);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const int d = threadIdx.x * 4 + k;
+      if (d < nd) digit_base[d] = v[k];
+    }
+  }
+  for (int d = lane; d < nd; d += 32) warp_hist[warp][d] = 0u;
+  __syncwarp();
+
+  const unsigned lt_mask = (1u << lane) - 1u;
+  uint32_t rank[kSortItems];
+#pragma unroll
+  for (int r = 0; r < kSortItems; ++r) {
+    const bool valid = base + r * 32 + lane < n;
+    const uint32_t digit = valid ? ((key[r] >> shift) & mask) : (uint32_t)nd;  // nd marks an empty slot
+    const unsigned peers = __match_any_sync(0xffffffffu, digit);
+    const uint32_t before = valid ? warp_hist[warp][digit] : 0u;
+    __syncwarp();
+    if (valid && lane == __ffs(peers) - 1) warp_hist[warp][digit] = before + __popc(peers);
+    __syncwarp();
+    rank[r] = before + __popc(peers & lt_mask);
+  }
+  __syncthreads();
+  // Per digit, exclusive prefix over the warps (warp order is item order within the tile).
+  for (int d = threadIdx.x; d < nd; d += kSortThreads) {
+    uint32_t run = digit_base[d] + counts[(size_t)d * max_tiles + t];
+#pragma unroll
+    for (int wi = 0; wi < kWarps; ++wi) {
+      const uint32_t c = warp_hist[wi][d];
+      warp_hist[wi][d] = run;
+      run += c;
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int r = 0; r < kSortItems; ++r) {
+    const int i = base + r * 32 + lane;
+    if (i < n) {
+      const uint32_t dst = warp_hist[warp][(key[r] >> shift) & mask] + rank[r];
+      const float4 rec = FROM_POS ? make_float4(px[FROM_POS ? r : 0], py[FROM_POS ? r : 0], w[i], __int_as_float(i))
+                                  : rec_in[i];
+      keys_out[dst] = key[r];
+      rec_out[dst] = rec;
+      if (FINAL) perm_out[dst] = (uint32_t)__float_as_int(rec.w);
     }
   }
 }
@@ -262,6 +420,51 @@ int launch_radix_sort(uint32_t* keys_a, uint32_t* vals_a, uint32_t* keys_b, uint
     uint32_t* tv = vin; vin = vout; vout = tv;
   }
   return (kin == keys_a) ? 0 : 1;  // which buffer pair holds the result
+}
+
+int record_sort_passes(int key_bits) { return key_bits <= kRecMaxBits ? 1 : (key_bits + kRecMaxBits - 1) / kRecMaxBits; }
+
+void launch_sort_records(const Geometry& g, const float2* pos, const float* w, const int* d_n, int max_n,
+                         int key_bits, float4* rec_final, float4* rec_tmp, uint32_t* key_final, uint32_t* key_tmp,
+                         uint32_t* perm, uint32_t* counts, uint32_t* digit_total, cudaStream_t stream) {
+  const int max_tiles = (max_n + kSortTile - 1) / kSortTile;
+  const int passes = record_sort_passes(key_bits);
+  const int per_pass = (key_bits + passes - 1) / passes;
+  const float4* rin = nullptr;
+  const uint32_t* kin = nullptr;
+  int shift = 0;
+  for (int p = 0; p < passes; ++p) {
+    const int bits = (shift + per_pass <= key_bits) ? per_pass : key_bits - shift;
+    const bool final_pass = p == passes - 1;
+    // Destinations alternate so that the last pass lands in the final buffers.
+    const bool to_final = ((passes - 1 - p) & 1) == 0;
+    float4* rout = to_final ? rec_final : rec_tmp;
+    uint32_t* kout = to_final ? key_final : key_tmp;
+    if (p == 0) {
+      rec_upsweep_kernel<true><<<max_tiles, kSortThreads, 0, stream>>>(g, pos, nullptr, d_n, shift, bits, counts,
+                                                                       max_tiles);
+    } else {
+      rec_upsweep_kernel<false><<<max_tiles, kSortThreads, 0, stream>>>(g, nullptr, kin, d_n, shift, bits, counts,
+                                                                        max_tiles);
+    }
+    radix_scan_kernel<<<1 << bits, kSortThreads, 0, stream>>>(counts, digit_total, d_n, max_tiles);
+    if (p == 0 && final_pass) {
+      rec_downsweep_kernel<true, true><<<max_tiles, kSortThreads, 0, stream>>>(
+          g, pos, w, nullptr, nullptr, kout, rout, perm, d_n, shift, bits, counts, digit_total, max_tiles);
+    } else if (p == 0) {
+      rec_downsweep_kernel<true, false><<<max_tiles, kSortThreads, 0, stream>>>(
+          g, pos, w, nullptr, nullptr, kout, rout, perm, d_n, shift, bits, counts, digit_total, max_tiles);
+    } else if (final_pass) {
+      rec_downsweep_kernel<false, true><<<max_tiles, kSortThreads, 0, stream>>>(
+          g, nullptr, nullptr, kin, rin, kout, rout, perm, d_n, shift, bits, counts, digit_total, max_tiles);
+    } else {
+      rec_downsweep_kernel<false, false><<<max_tiles, kSortThreads, 0, stream>>>(
+          g, nullptr, nullptr, kin, rin, kout, rout, perm, d_n, shift, bits, counts, digit_total, max_tiles);
+    }
+    rin = rout;
+    kin = kout;
+    shift += bits;
+  }
 }
 
 void launch_head(const uint32_t* keys, const int* d_n, int num_cells, int* head, int* d_n_alive,

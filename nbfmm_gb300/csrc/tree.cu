@@ -2,7 +2,7 @@
 // and postdo used by the stage entry points.
 //
 // Reference stages replaced (source/nbfmm/core/solver/):
-//   permuteInputVector  predo.cu:86-100    fused with P2M below (one pass over the sorted particles)
+//   permuteInputVector  predo.cu:86-100    the record sort (sort.cu) carries x, y, m through its passes
 //   p2m                 p2m.cu:24-110      per-cell sums by one warp in sorted order, no reduce_by_key, no host sync
 //   m2m                 m2m.cu:22-74       one thread per parent cell, compact per-level layout
 //   m2l                 m2l.cu:24-81       16x16 target tile per CTA with its 20x20 source halo in shared memory
@@ -18,33 +18,6 @@ namespace nbfmm_gb300 {
 namespace {
 
 constexpr int kCellWarps = 8;  // warps per CTA of the one-warp-per-cell kernels
-
-__global__ void gather_p2m_kernel(int num_cells, const int* __restrict__ head, const uint32_t* __restrict__ perm,
-                                  const float2* __restrict__ pos, const float* __restrict__ w,
-                                  float4* __restrict__ sorted4, float4* __restrict__ cell0) {
-  __shared__ float4 sums[kCellWarps][32];
-  const int lane = threadIdx.x & 31;
-  const int nwarps = (gridDim.x * blockDim.x) >> 5;
-  for (int c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; c < num_cells; c += nwarps) {
-    const int h0 = head[c], h1 = head[c + 1];
-    float acc = 0.0f;
-    for (int base = h0; base < h1; base += 32) {
-      const int i = base + lane;
-      float2 q = make_float2(0.0f, 0.0f);
-      float m = 0.0f;
-      if (i < h1) {
-        const uint32_t p = perm[i];
-        q = pos[p];
-        m = w[p];
-        sorted4[i] = make_float4(q.x, q.y, m, __int_as_float((int)p));
-      }
-      cell_sums_add_chunk(acc, sums[threadIdx.x >> 5], q.x, q.y, m, min(32, h1 - base), lane);
-    }
-    float sx, sy, sw;
-    cell_sums_get(acc, sx, sy, sw);
-    if (lane == 0) cell0[c] = centre_of_mass(sx, sy, sw, h1 > h0);
-  }
-}
 
 __global__ void p2m_kernel(int num_cells, const int* __restrict__ head, const float4* __restrict__ sorted4,
                            float4* __restrict__ cell0) {
@@ -141,13 +114,6 @@ int grid_for(long long n, int threads, int cap) {
 }
 
 }  // namespace
-
-void launch_gather_p2m(const Geometry& g, const int* head, const uint32_t* perm, const float2* pos,
-                       const float* w, float4* sorted4, float4* cell0, cudaStream_t stream) {
-  const int cells = g.base_dim * g.base_dim;
-  gather_p2m_kernel<<<grid_for((long long)cells * 32, kCellWarps * 32, 152 * 16), kCellWarps * 32, 0, stream>>>(
-      cells, head, perm, pos, w, sorted4, cell0);
-}
 
 void launch_p2m(const Geometry& g, const int* head, const float4* sorted4, float4* cell0, cudaStream_t stream) {
   const int cells = g.base_dim * g.base_dim;

@@ -228,6 +228,18 @@ def ref_lib():
     if L.ref_has_display():
         L.ref_display_device.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_float, _f, _f, _f, _u8]
         L.ref_display_device.restype = None
+    L.ref_has_prune.restype = ctypes.c_int
+    if L.ref_has_prune():
+        L.ref_prune.argtypes = [ctypes.c_int, _f, _f, _f, _f]
+        L.ref_prune.restype = ctypes.c_int
+    L.ref_has_models.restype = ctypes.c_int
+    if L.ref_has_models():
+        f = ctypes.c_float
+        for name, nf in (("circle_center", 6), ("circle_uniform_center", 6), ("disk", 5), ("disk_center", 6),
+                         ("disk_static", 4), ("rectangle", 6)):
+            fn = getattr(L, "ref_model_" + name)
+            fn.argtypes = [ctypes.c_int] + [f] * nf + [_f, _f, _f, _f]
+            fn.restype = None
     return L
 
 
@@ -260,6 +272,42 @@ def ref_display(pos, w, width, height, size_scale, limits, pad_rows=8):
     view = buf[pad:]
     L.ref_display_device(len(pos) // 2, width, height, float(size_scale), lim(limits), pos, f32(w), view)
     return buf[pad:pad + fb].copy(), int(np.count_nonzero(buf[:pad] != 7)), int(np.count_nonzero(buf[pad + fb:] != 7))
+
+
+def ref_prune(cur, prev, w, limits):
+    """The reference's Stars::prune (pruneDevice + thrust::sort_by_key on thrust's host system, oracle/_ref) in
+    place; returns the number of survivors, or None when oracle/_ref was not built."""
+    L = ref_lib()
+    if L is None or not L.ref_has_prune():
+        return None
+    return L.ref_prune(len(w), lim(limits), cur.reshape(-1), prev.reshape(-1), w)
+
+
+def ref_model(kind, n, u, **p):
+    """The reference's generate*Device kernel of one model (oracle/_ref) on draws u (n x 3): (cur, prev, w), or
+    None when oracle/_ref was not built. The double disks are two disks plus host-side offsets: not here."""
+    L = ref_lib()
+    if L is None or not L.ref_has_models():
+        return None
+    cur = np.zeros((n, 2), np.float32)
+    prev = np.zeros((n, 2), np.float32)
+    w = np.zeros(n, np.float32)
+    uu = f32(u).reshape(-1)
+    c = p["center"]
+    if kind in ("circle_center", "circle_uniform_center"):
+        args = (*c, p["radius"], p["weight"], p["center_weight"], p["tick"])
+    elif kind == "disk":
+        args = (*c, p["radius"], p["weight"], p["tick"])
+    elif kind == "disk_center":
+        args = (*c, p["radius"], p["weight"], p["center_weight"], p["tick"])
+    elif kind == "disk_static":
+        args = (*c, p["radius"], p["weight"])
+    elif kind == "rectangle":
+        args = (*c, p["width"], p["height"], p["max_weight"], p["tick"])
+    else:
+        raise ValueError(kind)
+    getattr(L, "ref_model_" + kind)(n, *[float(a) for a in args], uu, cur.reshape(-1), prev.reshape(-1), w)
+    return cur, prev, w
 
 
 def prune(cur, prev, w, limits):

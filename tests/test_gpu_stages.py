@@ -68,6 +68,37 @@ def test_predo(solver, golden, orc):
     np.testing.assert_array_equal(part[:, 3].view(np.int32), perm)
 
 
+@pytest.mark.parametrize("num_level,n", [(0, 5000), (1, 4097), (4, 100000), (5, 4096 * 3 + 17), (8, 700000),
+                                         (9, 1000003), (10, 2000000)])
+def test_predo_record_sort_across_depths(engine, orc, num_level, n):
+    """predo's record sort carries (x, y, m, index) through one (depth <= 5, keys of <= 10 bits), two (depth
+    6-10, keys of 12-20 bits) or three (depth 11, 22 bits) passes of up to 10-bit digits: every sorted record, key, permutation
+    entry and head equals the oracle's stable counting sort, on clustered positions (some cells empty, some
+    crowded, some particles on or outside the limits)."""
+    import torch
+
+    rng = np.random.default_rng(num_level * 1000 + 7)
+    lim = (-1.0, -2.0, 3.0, 1.0)
+    pos = np.concatenate([rng.normal(0.2, 0.4, (n // 2, 2)), rng.uniform(-1.5, 3.5, (n - n // 2, 2))])
+    pos = pos.astype(np.float32)
+    pos[:7] = [[-1, -2], [3, 1], [3, -2], [-1, 1], [9, 9], [-9, -9], [np.nan, 0.5]]
+    w = rng.uniform(0.5, 1.5, n).astype(np.float32)
+    s = engine.Solver(num_level, n, lim)
+    s.predo(n, to_gpu(pos), to_gpu(w))
+    torch.cuda.synchronize()
+    buf = s.buffers()
+    ref = orc.predo(pos, w, num_level, lim)
+    b = 1 << (num_level + 1)
+    perm = buf["perm"][:n].cpu().numpy()
+    np.testing.assert_array_equal(perm, ref["perm"])
+    np.testing.assert_array_equal(buf["head"].cpu().numpy(), ref["head"])
+    np.testing.assert_array_equal(buf["cell_key"][:n].cpu().numpy(), ref["index"][:, 0] + ref["index"][:, 1] * b)
+    part = buf["particle"][:n].cpu().numpy()
+    np.testing.assert_array_equal(part[:, 0:2].view(np.int32), pos[perm].view(np.int32))  # NaN bits too
+    np.testing.assert_array_equal(part[:, 2], w[perm])
+    np.testing.assert_array_equal(part[:, 3].view(np.int32), perm)
+
+
 def test_postdo(solver, golden):
     import torch
 

@@ -263,3 +263,61 @@ def test_threaded_display_equals_sequential(orc):
     a = orc.display(pos, w, 320, 200, 0.01, (-1, -1, 1, 1))
     b = orc.display(pos, w, 320, 200, 0.01, (-1, -1, 1, 1), threads=True)
     np.testing.assert_array_equal(a, b)
+
+
+@pytest.mark.parametrize("seed", [4, 5])
+def test_prune_matches_reference_library(orc, seed):
+    """The oracle's prune against the reference's own Stars::prune compiled for the CPU (oracle/_ref): its
+    pruneDevice flags and thrust::sort_by_key over the zipped (cur, prev, w) arrays on thrust's host system,
+    then thrust::find of the first flag (prune.cu:28-62). Same survivor count and the same arrays, bit for bit,
+    with NaN, infinite and on-the-limit positions."""
+    if orc.ref_prune(np.zeros((1, 2), np.float32), np.zeros((1, 2), np.float32), np.zeros(1, np.float32),
+                     (-1, -1, 1, 1)) is None:
+        pytest.skip("oracle/_ref not built (reference sources absent)")
+    rng = np.random.default_rng(seed)
+    n = 20000
+    cur = rng.uniform(-1.3, 1.3, (n, 2)).astype(np.float32)
+    cur[::101] = np.nan
+    cur[5::211] = [np.inf, 0.0]
+    cur[7::307] = [-1.0, 1.0]   # on the limits: kept (prune.cu:40-41 tests < and >)
+    cur[9::401] = [0.0, -np.inf]
+    prev = rng.normal(size=(n, 2)).astype(np.float32)
+    w = rng.uniform(size=n).astype(np.float32)
+    limits = (-1.0, -1.0, 1.0, 1.0)
+    a = [cur.copy(), prev.copy(), w.copy()]
+    b = [cur.copy(), prev.copy(), w.copy()]
+    assert orc.prune(*a, limits) == orc.ref_prune(*b, limits)
+    for x, y in zip(a, b):
+        np.testing.assert_array_equal(x.view(np.int32), y.view(np.int32))
+
+
+MODEL_PARAMS = dict(center=(0.3, -0.2), radius=1.7, weight=1e-3, center_weight=5.0, tick=1e-3, width=2.0,
+                    height=3.0, max_weight=2.0)
+
+
+@pytest.mark.parametrize("kind", ["circle_center", "circle_uniform_center", "disk", "disk_center", "disk_static",
+                                  "rectangle"])
+def test_models_match_reference_kernels(orc, kind):
+    """The oracle's model arithmetic against the reference's own generate*Device kernels compiled for the CPU
+    (oracle/_ref), curand bound to the same uniform draws. Weights are equal; each coordinate is within one ulp
+    of the coordinate scale (|centre| + the largest extent): the oracle rounds center + radius * cos(angle) once, as the
+    CUDA compiler's fused multiply-add does, and the CPU build of the kernel rounds the product and the sum
+    separately. The rectangle's x and y draws are two curand_uniform calls in one make_float2 argument list,
+    whose evaluation order C++ leaves unspecified: g++ evaluates the y draw first, the oracle (and the engine)
+    take the x draw first, so the reference is given the draws in that order."""
+    if orc.ref_model(kind, 1, np.zeros((1, 3), np.float32), **MODEL_PARAMS) is None:
+        pytest.skip("oracle/_ref not built (reference sources absent)")
+    rng = np.random.default_rng(len(kind))
+    n = 20000
+    u = rng.uniform(0, 1, (n, 3)).astype(np.float32)
+    u_ref = u.copy()
+    if kind == "rectangle":
+        u_ref[:, [0, 1]] = u_ref[:, [1, 0]]
+    ours = orc.model(kind, n, u, **MODEL_PARAMS)
+    ref = orc.ref_model(kind, n, u_ref, **MODEL_PARAMS)
+    scale = np.float32(abs(MODEL_PARAMS["center"][0]) + abs(MODEL_PARAMS["center"][1]) +
+                       max(MODEL_PARAMS["radius"], MODEL_PARAMS["width"], MODEL_PARAMS["height"]))
+    tol = np.spacing(scale)
+    for name, a, b in zip(("cur", "prev"), ours[:2], ref[:2]):
+        assert np.abs(a - b).max() <= tol, f"{name}: {np.abs(a - b).max() / np.spacing(scale):.3f} ulp"
+    np.testing.assert_array_equal(ours[2], ref[2])
