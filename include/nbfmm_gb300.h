@@ -259,7 +259,7 @@ int nbfmm_model_set_uniforms(const float* gpuptr_uniforms);
 /* No counterpart in the reference. The leaf-cell sort of predo (cell keys, stable sort, heads) for callers
  * that cannot allocate device memory: a plugin whose host application owns every device buffer, or code
  * that must not trigger cudaMalloc's device synchronisation. It allocates nothing; its scratch is a fixed
- * device array inside the library (about 4.5 MB per GPU that loads it, held until exit), so at most 262,144
+ * device array inside the library (about 4.1 MB per GPU that loads it, held until exit), so at most 262,144
  * particles per call, and calls that overlap on the GPU race on that shared scratch. Every call looks the
  * scratch address up in the current CUDA context (cudaGetSymbolAddress, which neither allocates nor
  * synchronises), so a context the host makes current, or a device reset, is followed; the first call on each

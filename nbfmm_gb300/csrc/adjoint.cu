@@ -465,7 +465,17 @@ struct nbfmm_adjoint {
   float *gm = nullptr, *gm_acc = nullptr, *loss_terms = nullptr;
   float2* cell_lam = nullptr;
   float4* cell_g = nullptr;
+  // Per step of a segment, the sort of that step's positions as its recomputation left it (sorted particles,
+  // permutation, heads, cell centres of every level), reused by the step's vector-Jacobian product.
+  float4* slot_sorted = nullptr;
+  uint32_t* slot_perm = nullptr;
+  int* slot_head = nullptr;
+  float4* slot_cell = nullptr;
   const float* m = nullptr;  // caller's masses, kept between forward and backward
+  float4* own_sorted = nullptr;  // the solver's own sort outputs (bind_slot)
+  uint32_t* own_vals = nullptr;
+  int* own_head = nullptr;
+  float4* own_cell = nullptr;
   float fwd_ms = 0.0f, bwd_ms = 0.0f;
 
   int init(int num_level, int num_particle, const float* limits, float tau_, int max_steps_, int k_) {
@@ -490,16 +500,44 @@ struct nbfmm_adjoint {
     NBFMM_TRY(dalloc(&loss_terms, N, "loss terms"));
     NBFMM_TRY(dalloc(&cell_lam, (size_t)solver->lv.total, "cell adjoints"));
     NBFMM_TRY(dalloc(&cell_g, (size_t)solver->lv.total, "cell gradients"));
+    NBFMM_TRY(dalloc(&slot_sorted, N * k, "segment sorted particles"));
+    NBFMM_TRY(dalloc(&slot_perm, N * k, "segment permutations"));
+    NBFMM_TRY(dalloc(&slot_head, ((size_t)solver->num_cells + 2) * k, "segment heads"));
+    NBFMM_TRY(dalloc(&slot_cell, (size_t)solver->lv.total * k, "segment cells"));
+    own_sorted = solver->sorted4;
+    own_vals = solver->vals_a;
+    own_head = solver->head;
+    own_cell = solver->cell4;
     return cuda_check("adjoint init");
   }
 
   ~nbfmm_adjoint() {
     dfree(x); dfree(xp); dfree(acc); dfree(ckpt); dfree(seg); dfree(lam_a); dfree(lam_b); dfree(gx); dfree(smu);
     dfree(gm); dfree(gm_acc); dfree(loss_terms); dfree(cell_lam); dfree(cell_g);
+    dfree(slot_sorted); dfree(slot_perm); dfree(slot_head); dfree(slot_cell);
     delete solver;
   }
 
   float2* ck(int i, int which) { return ckpt + ((size_t)i * 2 + which) * (size_t)n; }
+
+  // Points the solver's sort outputs at segment slot `slot` (or back at its own buffers with slot < 0).
+  void bind_slot(int slot) {
+    nbfmm_solver& v = *solver;
+    if (slot < 0) {
+      v.sorted4 = own_sorted;
+      v.vals_a = own_vals;
+      v.head = own_head;
+      v.cell4 = own_cell;
+      v.perm = own_vals;
+      return;
+    }
+    const size_t N = (size_t)std::max(n, 1);
+    v.sorted4 = slot_sorted + slot * N;
+    v.vals_a = slot_perm + slot * N;
+    v.head = slot_head + slot * ((size_t)v.num_cells + 2);
+    v.cell4 = slot_cell + slot * (size_t)v.lv.total;
+    v.perm = v.vals_a;
+  }
 
   void step(cudaStream_t s) {  // one forward step on (x, xp)
     solver->solve(n, reinterpret_cast<const float*>(x), m, reinterpret_cast<float*>(acc), s);
@@ -522,16 +560,19 @@ struct nbfmm_adjoint {
     return cuda_check("nbfmm_adjoint_forward");
   }
 
-  // VJP of one solve at positions `pos` (original order) for effect adjoint scale * lam; results in gx, gm.
-  void vjp(const float2* pos, const float2* lam, float scale, cudaStream_t s) {
+  // VJP of one solve at positions `pos` (original order) for effect adjoint scale * lam; results in gx, gm. With
+  // `cached`, the solver is bound to the slot the step's recomputation sorted pos into (bind_slot), and only the
+  // work list is rebuilt (the solve's pairs tails; adj_p2p_kernel reads plain 128-target chunks).
+  void vjp(const float2* pos, const float2* lam, float scale, bool cached, cudaStream_t s) {
     nbfmm_solver& v = *solver;
-    v.predo(n, pos, m, s, false);  // adj_p2p_kernel reads plain 128-target chunks
+    if (cached) launch_worklist(v.head, v.num_cells, v.work, v.d_work_count(), false, s);
+    else v.predo(n, pos, m, s, false);
     const int cells = v.num_cells;
     adj_gather_kernel<<<grid_for((long long)cells * 32, 256, 152 * 16), 256, 0, s>>>(cells, v.head, v.perm, lam,
                                                                                     scale, smu, cell_lam);
     const bool far = v.geo.num_level > 0;
     if (far) {
-      launch_m2m(v.lv, v.cell4, s);
+      if (!cached) launch_m2m(v.lv, v.cell4, s);  // a cached slot holds every level
       for (int l = 1; l < v.lv.count; ++l) {
         adj_up_kernel<<<grid_for((long long)v.lv.dim[l] * v.lv.dim[l], 256, 152 * 8), 256, 0, s>>>(
             cell_lam, v.lv.offset[l - 1], v.lv.dim[l - 1], v.lv.offset[l], v.lv.dim[l]);
@@ -574,12 +615,18 @@ struct nbfmm_adjoint {
       const int t0 = sgi * k, t1 = std::min(t0 + k, steps);
       cudaMemcpyAsync(x, ck(sgi, 0), sizeof(float2) * N, cudaMemcpyDeviceToDevice, s);
       cudaMemcpyAsync(xp, ck(sgi, 1), sizeof(float2) * N, cudaMemcpyDeviceToDevice, s);
-      for (int t = t0; t < t1; ++t) {  // positions x_t for t in [t0, t1)
+      for (int t = t0; t < t1; ++t) {  // positions x_t for t in [t0, t1); each step's sort kept in its slot
         cudaMemcpyAsync(seg + (size_t)(t - t0) * N, x, sizeof(float2) * N, cudaMemcpyDeviceToDevice, s);
-        if (t + 1 < t1) step(s);
+        if (t + 1 < t1) {
+          bind_slot(t - t0);
+          step(s);
+          bind_slot(-1);
+        }
       }
       for (int t = t1 - 1; t >= t0; --t) {
-        vjp(seg + (size_t)(t - t0) * N, lam_a, tau2, s);
+        bind_slot(t - t0);
+        vjp(seg + (size_t)(t - t0) * N, lam_a, tau2, t + 1 < t1, s);
+        bind_slot(-1);
         adj_step_kernel<<<grid_for(N, 256, 152 * 16), 256, 0, s>>>(N, lam_a, lam_b, gx, gm, gm_acc);
         std::swap(lam_a, lam_b);  // lam_a = lambda_t, lam_b = lambda_{t+1}
       }

@@ -23,8 +23,10 @@ constexpr int kMaxLevels = 11;           // num_level in [0, 10], B <= 2048
 constexpr int kSortThreads = 256;        // radix sort CTA
 constexpr int kSortItems = 16;           // items per thread
 constexpr int kSortTile = kSortThreads * kSortItems;  // 4096 items per tile
-constexpr int kRadixMaxBits = 10;        // digit bits per pass of the (key, value) radix sort: 2 passes for 20 bits
+constexpr int kRadixMaxBits = 8;         // digit bits per pass of the (key, value) radix sort
 constexpr int kRecMaxBits = 10;          // digit bits per pass of the record sort (launch_sort_records)
+constexpr int kRecItems = 16;            // record sort: items per thread
+constexpr int kRecTile = kSortThreads * kRecItems;  // 4096 items per tile
 constexpr int kP2PThreads = 128;        // 4 independent warps per CTA
 constexpr int kP2PPasses = 4;            // targets per lane in one work item (4 passes of 32)
 constexpr int kP2PChunk = 32 * kP2PPasses;  // targets per work item
@@ -185,7 +187,7 @@ int launch_radix_sort(uint32_t* keys_a, uint32_t* vals_a, uint32_t* keys_b, uint
 // Stable LSD radix sort of caller-order particles by leaf key, carrying each particle's record: on return
 // rec_final[i] = (x, y, m, original index bits), key_final[i] its leaf key and perm[i] its original index, in
 // key order (ties in caller order). rec_tmp / key_tmp hold the passes in between. counts needs
-// 2^kRecMaxBits * ceil(max_n / kSortTile) words and digit_total 2^kRecMaxBits.
+// 2^kRecMaxBits * ceil(max_n / kRecTile) words and digit_total 2^kRecMaxBits.
 int record_sort_passes(int key_bits);
 void launch_sort_records(const Geometry& g, const float2* pos, const float* w, const int* d_n, int max_n,
                          int key_bits, float4* rec_final, float4* rec_tmp, uint32_t* key_final, uint32_t* key_tmp,
@@ -214,6 +216,10 @@ void launch_m2m(const Levels& lv, float4* cell4, cudaStream_t stream);
 
 // M2L on every level; with `with_l2l` the parent effect is added on the way down (M2L + L2L fused).
 void launch_m2l(const Levels& lv, const float4* cell4, float2* ceff, float eps, bool with_l2l, cudaStream_t stream);
+
+// The far field of a solve: M2M up every level, then M2L with L2L fused down every level. The levels of at most
+// 32 cells per side run in one launch.
+void launch_far_field(const Levels& lv, float4* cell4, float2* ceff, float eps, cudaStream_t stream);
 
 // L2L alone (stage entry point).
 void launch_l2l(const Levels& lv, float2* ceff, cudaStream_t stream);

@@ -7,7 +7,7 @@
 // GPU with other streams). nbfmm_solver_create allocates the whole workspace up front; this entry point
 // instead keeps its sort scratch in one file-scope device array, so a call allocates nothing at all.
 //
-// Limits and sharing: at most kNoAllocMaxParticles particles per call (scratch ~4.5 MB, held by every GPU
+// Limits and sharing: at most kNoAllocMaxParticles particles per call (scratch ~4.1 MB, held by every GPU
 // that loads the library until the process exits). Every call on a device uses the same array, which keeps
 // the last call's contents; nothing in it has to start at zero (each call writes every scratch word it
 // reads), but calls that overlap on the GPU -- on two streams, or from two host threads -- race on it.

@@ -126,7 +126,8 @@ struct nbfmm_solver {
     NBFMM_TRY(dalloc(&keys_b, n, "keys"));
     NBFMM_TRY(dalloc(&vals_b, n, "values"));
     constexpr int kDigits = 1 << (kRecMaxBits > kRadixMaxBits ? kRecMaxBits : kRadixMaxBits);
-    NBFMM_TRY(dalloc(&counts, (size_t)kDigits * max_tiles, "tile counts"));
+    const size_t count_tiles = (size_t)(max_n + kRecTile - 1) / kRecTile;  // >= the key/value sort's tiles
+    NBFMM_TRY(dalloc(&counts, (size_t)kDigits * count_tiles, "tile counts"));
     NBFMM_TRY(dalloc(&digit_total, (size_t)kDigits, "digit totals"));
     NBFMM_TRY(dalloc(&head, (size_t)num_cells + 2, "head"));
     NBFMM_TRY(dalloc(&work, work_list_capacity(num_cells, n), "work list"));
@@ -178,8 +179,7 @@ struct nbfmm_solver {
 
   void far_field(cudaStream_t s) {
     if (geo.num_level <= 0) return;  // p2m.cu:80, m2l.cu:64
-    launch_m2m(lv, cell4, s);         // no-op for num_level <= 1 (m2m.cu:60)
-    launch_m2l(lv, cell4, ceff, eps, true, s);
+    launch_far_field(lv, cell4, ceff, eps, s);  // M2M is a no-op for num_level <= 1 (m2m.cu:60)
   }
 
   P2PArgs p2p_args() {

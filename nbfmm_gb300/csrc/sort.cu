@@ -7,9 +7,12 @@
 // equals the order of the integer key iy*B + ix, and cub's merge sort keeps equal keys in input order, so a
 // stable radix sort on that key reproduces the reference's permutation bit for bit.
 //
-// Sort design: per pass (digits of up to 10 bits), an upsweep writes each 4096-item tile's digit histogram, one
+// Sort design: per pass (digits of up to 8 bits), an upsweep writes each 4096-item tile's digit histogram, one
 // CTA per digit scans its row of tile counts, and a downsweep ranks each tile's items stably (warp match +
-// per-warp digit counters in shared memory) and scatters them. Every kernel reads the element count from device memory,
+// per-warp digit counters in shared memory) and scatters them. On the step's nearly sorted state, 8-bit digits
+// in three passes were measured faster than 10-bit digits in two (0.33 against 0.38 ms at 16.8M): narrower
+// digits keep longer runs of a tile together in one store. Loading each round's keys and values inside the
+// ranking loop was measured faster here than loading the whole tile first (0.09 against 0.13 ms per pass). Every kernel reads the element count from device memory,
 // so the same launches serve any n <= max_n without a host round trip (and can be captured in a graph).
 #include "engine.cuh"
 
@@ -17,7 +20,7 @@ namespace nbfmm_gb300 {
 
 namespace {
 
-__device__ __forceinline__ int num_tiles(int n) { return (n + kSortTile - 1) / kSortTile; }
+__device__ __forceinline__ int num_tiles(int n, int tile = kSortTile) { return (n + tile - 1) / tile; }
 
 // Exclusive scan over a 256-thread block; returns the block total in *total.
 __device__ __forceinline__ uint32_t block_exclusive_scan_256(uint32_t v, uint32_t* warp_sums, uint32_t* total) {
@@ -93,9 +96,9 @@ radix_upsweep_kernel(const uint32_t* __restrict__ keys, const int* __restrict__ 
 // One CTA per digit: exclusive scan of that digit's tile counts; the digit's total goes to digit_total.
 __global__ void __launch_bounds__(kSortThreads)
 radix_scan_kernel(uint32_t* __restrict__ counts, uint32_t* __restrict__ digit_total, const int* __restrict__ d_n,
-                  int max_tiles) {
+                  int max_tiles, int tile = kSortTile) {
   __shared__ uint32_t warp_sums[kSortThreads / 32];
-  const int nt = num_tiles(*d_n);
+  const int nt = num_tiles(*d_n, tile);
   uint32_t* row = counts + (size_t)blockIdx.x * max_tiles;
   uint32_t carry = 0;
   for (int base = 0; base < nt; base += kSortThreads * 4) {
@@ -133,38 +136,26 @@ radix_downsweep_kernel(const uint32_t* __restrict__ keys_in, const uint32_t* __r
   const int lane = threadIdx.x & 31;
   const int warp = threadIdx.x >> 5;
 
-  // Start of every digit in the output: exclusive scan of the digit totals (4 digits per thread).
+  // Start of every digit in the output: exclusive scan of the digit totals.
   {
-    uint32_t v[4];
-#pragma unroll
-    for (int k = 0; k < 4; ++k) {
-      const int d = threadIdx.x * 4 + k;
-      v[k] = d < nd ? digit_total[d] : 0u;
-    }
-    block_exclusive_scan_4x256(v, warp_sums);
-#pragma unroll
-    for (int k = 0; k < 4; ++k) {
-      const int d = threadIdx.x * 4 + k;
-      if (d < nd) digit_base[d] = v[k];
-    }
+    const uint32_t v = (threadIdx.x < nd) ? digit_total[threadIdx.x] : 0u;
+    uint32_t total;
+    const uint32_t ex = block_exclusive_scan_256(v, warp_sums, &total);
+    if (threadIdx.x < nd) digit_base[threadIdx.x] = ex;
   }
   for (int d = lane; d < nd; d += 32) warp_hist[warp][d] = 0u;
   __syncwarp();
 
-  // Warp `warp` owns items [warp*512, warp*512 + 512) of the tile, in 16 rounds of 32 consecutive items. The
-  // keys are all loaded before the ranking (16 loads per thread in flight); values are read when scattered.
+  // Warp `warp` owns items [warp*512, warp*512 + 512) of the tile, in 16 rounds of 32 consecutive items.
   const int base = t * kSortTile + warp * (32 * kSortItems);
   const unsigned lt_mask = (1u << lane) - 1u;
-  uint32_t key[kSortItems], rank[kSortItems];
-#pragma unroll
-  for (int r = 0; r < kSortItems; ++r) {
-    const int i = base + r * 32 + lane;
-    key[r] = i < n ? keys_in[i] : 0u;
-  }
+  uint32_t key[kSortItems], val[kSortItems], rank[kSortItems];
 #pragma unroll
   for (int r = 0; r < kSortItems; ++r) {
     const int i = base + r * 32 + lane;
     const bool valid = i < n;
+    key[r] = valid ? keys_in[i] : 0u;
+    val[r] = valid ? vals_in[i] : 0u;
     const uint32_t digit = valid ? ((key[r] >> shift) & mask) : (uint32_t)nd;  // nd marks an empty slot
     const unsigned peers = __match_any_sync(0xffffffffu, digit);
     const uint32_t before = valid ? warp_hist[warp][digit] : 0u;
@@ -192,9 +183,21 @@ radix_downsweep_kernel(const uint32_t* __restrict__ keys_in, const uint32_t* __r
       const uint32_t digit = (key[r] >> shift) & mask;
       const uint32_t dst = warp_hist[warp][digit] + rank[r];
       keys_out[dst] = key[r];
-      vals_out[dst] = vals_in[i];
+      vals_out[dst] = val[r];
     }
   }
+}
+
+// 16-byte asynchronous copy from global to shared memory (no register round trip); completed by
+// cp_async_wait_all.
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+  const unsigned dst = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(gmem) : "memory");
+}
+
+__device__ __forceinline__ void cp_async_wait_all() {
+  asm volatile("cp.async.commit_group;" ::: "memory");
+  asm volatile("cp.async.wait_group 0;" ::: "memory");
 }
 
 // ---- Record sort: the solve's predo ----------------------------------------------------------------------
@@ -214,13 +217,13 @@ rec_upsweep_kernel(Geometry g, const float2* __restrict__ pos, const uint32_t* _
   __shared__ uint32_t hist[1 << kRecMaxBits];
   const int n = *d_n;
   const int t = blockIdx.x;
-  if (t >= num_tiles(n)) return;
+  if (t >= num_tiles(n, kRecTile)) return;
   const int nd = 1 << bits;
   const uint32_t mask = (uint32_t)nd - 1u;
   for (int d = threadIdx.x; d < nd; d += kSortThreads) hist[d] = 0u;
   __syncthreads();
-  const int base = t * kSortTile;
-  const int end = min(base + kSortTile, n);
+  const int base = t * kRecTile;
+  const int end = min(base + kRecTile, n);
   for (int i = base + threadIdx.x; i < end; i += kSortThreads) {
     uint32_t key;
     if (FROM_POS) {
@@ -235,6 +238,17 @@ rec_upsweep_kernel(Geometry g, const float2* __restrict__ pos, const uint32_t* _
   for (int d = threadIdx.x; d < nd; d += kSortThreads) counts[(size_t)d * max_tiles + t] = hist[d];
 }
 
+// Tiles of kRecTile items, kRecItems per thread, the keys (or positions) of the tile loaded before the ranking.
+// The tile is then staged in shared memory in digit order and written out
+// with consecutive threads on consecutive items, so that a digit's run of the tile leaves in one coalesced
+// store. (Scattering from registers sends each warp store to ~32 different places, and a profile showed those
+// scattered stores, not DRAM, bounding the kernel: about one memory transaction per item and array.)
+// Dynamic shared memory: per-warp digit counters [kWarps][nd], the tile's digit starts [nd], the global offset of
+// each digit's run [nd], staged keys [kRecTile] and records [kRecTile].
+__host__ __device__ constexpr int rec_smem_bytes(int nd) {
+  return (kSortThreads / 32) * nd * 4 + 2 * nd * 4 + kRecTile * 4 + kRecTile * 16;
+}
+
 template <bool FROM_POS, bool FINAL>
 __global__ void __launch_bounds__(kSortThreads, 2)
 rec_downsweep_kernel(Geometry g, const float2* __restrict__ pos, const float* __restrict__ w,
@@ -243,90 +257,118 @@ rec_downsweep_kernel(Geometry g, const float2* __restrict__ pos, const float* __
                      const int* __restrict__ d_n, int shift, int bits, const uint32_t* __restrict__ counts,
                      const uint32_t* __restrict__ digit_total, int max_tiles) {
   constexpr int kWarps = kSortThreads / 32;
-  __shared__ uint32_t warp_hist[kWarps][1 << kRecMaxBits];
-  __shared__ uint32_t digit_base[1 << kRecMaxBits];
+  extern __shared__ __align__(16) unsigned char rec_smem[];
   __shared__ uint32_t warp_sums[kWarps];
   const int n = *d_n;
   const int t = blockIdx.x;
-  if (t >= num_tiles(n)) return;
+  if (t >= num_tiles(n, kRecTile)) return;
   const int nd = 1 << bits;
   const uint32_t mask = (uint32_t)nd - 1u;
   const int lane = threadIdx.x & 31;
   const int warp = threadIdx.x >> 5;
+  uint32_t* warp_hist = reinterpret_cast<uint32_t*>(rec_smem);  // [kWarps][nd]
+  uint32_t* local_start = warp_hist + kWarps * nd;               // [nd]
+  uint32_t* delta = local_start + nd;                            // [nd]: global - local position of a digit's run
+  uint32_t* skey = delta + nd;                                   // [kRecTile]
+  float4* srec = reinterpret_cast<float4*>(skey + kRecTile);     // [kRecTile]
 
-  // The tile's keys (the first pass computes them from the positions and keeps x, y), loaded before any
-  // ranking so that all 16 loads per thread are in flight together; the rest of each record is read when it
-  // is scattered.
-  const int base = t * kSortTile + warp * (32 * kSortItems);
-  uint32_t key[kSortItems];
-  float px[FROM_POS ? kSortItems : 1], py[FROM_POS ? kSortItems : 1];
+  // Warp `warp` owns items [warp*256, warp*256 + 256) of the tile, in kRecItems rounds of 32 consecutive items.
+  const int tile0 = t * kRecTile;
+  const int tile_n = min(kRecTile, n - tile0);
+  const int base = tile0 + warp * (32 * kRecItems);
+  // The first pass keeps each record in registers (it computes the key from the position); later passes load
+  // the keys now and copy each record from global memory straight into its staged slot (cp.async) once its
+  // place is known.
+  uint32_t key[kRecItems];
+  float4 rec[FROM_POS ? kRecItems : 1];
 #pragma unroll
-  for (int r = 0; r < kSortItems; ++r) {
+  for (int r = 0; r < kRecItems; ++r) {
     const int i = base + r * 32 + lane;
     if (FROM_POS) {
-      const float2 p = (i < n) ? pos[i] : make_float2(0.0f, 0.0f);
-      px[r] = p.x;
-      py[r] = p.y;
-      key[r] = leaf_key(g, p.x, p.y);
+      float2 p = make_float2(0.0f, 0.0f);
+      float m = 0.0f;
+      if (i < n) {
+        p = pos[i];
+        m = w[i];
+      }
+      rec[FROM_POS ? r : 0] = make_float4(p.x, p.y, m, __int_as_float(i));
     } else {
       key[r] = (i < n) ? keys_in[i] : 0u;
     }
   }
-
-  // Start of every digit in the output: exclusive scan of the digit totals (4 digits per thread).
-  {
-    uint32_t v[4];
+  if (FROM_POS) {
 #pragma unroll
-    for (int k = 0; k < 4; ++k) {
-      const int d = threadIdx.x * 4 + k;
-      v[k] = d < nd ? digit_total[d] : 0u;
-    }
-    block_exclusive_scan_4x256(v, warp_sums);
-#pragma unroll
-    for (int k = 0; k < 4; ++k) {
-      const int d = threadIdx.x * 4 + k;
-      if (d < nd) digit_base[d] = v[k];
-    }
+    for (int r = 0; r < kRecItems; ++r) key[r] = leaf_key(g, rec[FROM_POS ? r : 0].x, rec[FROM_POS ? r : 0].y);
   }
-  for (int d = lane; d < nd; d += 32) warp_hist[warp][d] = 0u;
-  __syncwarp();
 
+  for (int d = lane; d < nd; d += 32) warp_hist[warp * nd + d] = 0u;
+  __syncwarp();
   const unsigned lt_mask = (1u << lane) - 1u;
-  uint32_t rank[kSortItems];
+  uint32_t rank[kRecItems];
 #pragma unroll
-  for (int r = 0; r < kSortItems; ++r) {
+  for (int r = 0; r < kRecItems; ++r) {
     const bool valid = base + r * 32 + lane < n;
     const uint32_t digit = valid ? ((key[r] >> shift) & mask) : (uint32_t)nd;  // nd marks an empty slot
     const unsigned peers = __match_any_sync(0xffffffffu, digit);
-    const uint32_t before = valid ? warp_hist[warp][digit] : 0u;
+    const uint32_t before = valid ? warp_hist[warp * nd + digit] : 0u;
     __syncwarp();
-    if (valid && lane == __ffs(peers) - 1) warp_hist[warp][digit] = before + __popc(peers);
+    if (valid && lane == __ffs(peers) - 1) warp_hist[warp * nd + digit] = before + __popc(peers);
     __syncwarp();
     rank[r] = before + __popc(peers & lt_mask);
   }
   __syncthreads();
-  // Per digit, exclusive prefix over the warps (warp order is item order within the tile).
-  for (int d = threadIdx.x; d < nd; d += kSortThreads) {
-    uint32_t run = digit_base[d] + counts[(size_t)d * max_tiles + t];
+  // Per digit (4 per thread): the tile's count, the warps' exclusive prefix within the digit, the digit's start in
+  // the staged tile (a block scan of the counts) and the offset from staged to global position: the digit's
+  // global start (scan of the digit totals) plus this tile's offset within the digit (the scanned tile counts).
+  {
+    uint32_t cnt[4], gstart[4];
 #pragma unroll
-    for (int wi = 0; wi < kWarps; ++wi) {
-      const uint32_t c = warp_hist[wi][d];
-      warp_hist[wi][d] = run;
-      run += c;
+    for (int k = 0; k < 4; ++k) {
+      const int d = threadIdx.x * 4 + k;
+      uint32_t run = 0u;
+      if (d < nd) {
+#pragma unroll
+        for (int wi = 0; wi < kWarps; ++wi) {
+          const uint32_t c = warp_hist[wi * nd + d];
+          warp_hist[wi * nd + d] = run;
+          run += c;
+        }
+      }
+      cnt[k] = run;
+      gstart[k] = d < nd ? digit_total[d] : 0u;
+    }
+    block_exclusive_scan_4x256(gstart, warp_sums);
+    block_exclusive_scan_4x256(cnt, warp_sums);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const int d = threadIdx.x * 4 + k;
+      if (d < nd) {
+        local_start[d] = cnt[k];
+        delta[d] = gstart[k] + counts[(size_t)d * max_tiles + t] - cnt[k];
+      }
     }
   }
   __syncthreads();
 #pragma unroll
-  for (int r = 0; r < kSortItems; ++r) {
+  for (int r = 0; r < kRecItems; ++r) {
     const int i = base + r * 32 + lane;
     if (i < n) {
-      const uint32_t dst = warp_hist[warp][(key[r] >> shift) & mask] + rank[r];
-      const float4 rec = FROM_POS ? make_float4(px[FROM_POS ? r : 0], py[FROM_POS ? r : 0], w[i], __int_as_float(i))
-                                  : rec_in[i];
-      keys_out[dst] = key[r];
-      rec_out[dst] = rec;
-      if (FINAL) perm_out[dst] = (uint32_t)__float_as_int(rec.w);
+      const uint32_t d = (key[r] >> shift) & mask;
+      const uint32_t l = local_start[d] + warp_hist[warp * nd + d] + rank[r];
+      skey[l] = key[r];
+      if (FROM_POS) srec[l] = rec[FROM_POS ? r : 0];
+      else cp_async16(&srec[l], &rec_in[i]);
     }
+  }
+  if (!FROM_POS) cp_async_wait_all();
+  __syncthreads();
+  for (int l = threadIdx.x; l < tile_n; l += kSortThreads) {
+    const uint32_t k = skey[l];
+    const uint32_t dst = (uint32_t)l + delta[(k >> shift) & mask];
+    const float4 q = srec[l];
+    keys_out[dst] = k;
+    rec_out[dst] = q;
+    if (FINAL) perm_out[dst] = (uint32_t)__float_as_int(q.w);
   }
 }
 
@@ -427,8 +469,14 @@ int record_sort_passes(int key_bits) { return key_bits <= kRecMaxBits ? 1 : (key
 void launch_sort_records(const Geometry& g, const float2* pos, const float* w, const int* d_n, int max_n,
                          int key_bits, float4* rec_final, float4* rec_tmp, uint32_t* key_final, uint32_t* key_tmp,
                          uint32_t* perm, uint32_t* counts, uint32_t* digit_total, cudaStream_t stream) {
-  const int max_tiles = (max_n + kSortTile - 1) / kSortTile;
+  const int max_tiles = (max_n + kRecTile - 1) / kRecTile;
   const int passes = record_sort_passes(key_bits);
+  // The kernels' dynamic shared-memory limit (a per-device function attribute; setting it is a host-side call).
+  const int most = rec_smem_bytes(1 << kRecMaxBits);
+  cudaFuncSetAttribute(rec_downsweep_kernel<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, most);
+  cudaFuncSetAttribute(rec_downsweep_kernel<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, most);
+  cudaFuncSetAttribute(rec_downsweep_kernel<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, most);
+  cudaFuncSetAttribute(rec_downsweep_kernel<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, most);
   const int per_pass = (key_bits + passes - 1) / passes;
   const float4* rin = nullptr;
   const uint32_t* kin = nullptr;
@@ -447,18 +495,19 @@ void launch_sort_records(const Geometry& g, const float2* pos, const float* w, c
       rec_upsweep_kernel<false><<<max_tiles, kSortThreads, 0, stream>>>(g, nullptr, kin, d_n, shift, bits, counts,
                                                                         max_tiles);
     }
-    radix_scan_kernel<<<1 << bits, kSortThreads, 0, stream>>>(counts, digit_total, d_n, max_tiles);
+    radix_scan_kernel<<<1 << bits, kSortThreads, 0, stream>>>(counts, digit_total, d_n, max_tiles, kRecTile);
+    const int smem = rec_smem_bytes(1 << bits);
     if (p == 0 && final_pass) {
-      rec_downsweep_kernel<true, true><<<max_tiles, kSortThreads, 0, stream>>>(
+      rec_downsweep_kernel<true, true><<<max_tiles, kSortThreads, smem, stream>>>(
           g, pos, w, nullptr, nullptr, kout, rout, perm, d_n, shift, bits, counts, digit_total, max_tiles);
     } else if (p == 0) {
-      rec_downsweep_kernel<true, false><<<max_tiles, kSortThreads, 0, stream>>>(
+      rec_downsweep_kernel<true, false><<<max_tiles, kSortThreads, smem, stream>>>(
           g, pos, w, nullptr, nullptr, kout, rout, perm, d_n, shift, bits, counts, digit_total, max_tiles);
     } else if (final_pass) {
-      rec_downsweep_kernel<false, true><<<max_tiles, kSortThreads, 0, stream>>>(
+      rec_downsweep_kernel<false, true><<<max_tiles, kSortThreads, smem, stream>>>(
           g, nullptr, nullptr, kin, rin, kout, rout, perm, d_n, shift, bits, counts, digit_total, max_tiles);
     } else {
-      rec_downsweep_kernel<false, false><<<max_tiles, kSortThreads, 0, stream>>>(
+      rec_downsweep_kernel<false, false><<<max_tiles, kSortThreads, smem, stream>>>(
           g, nullptr, nullptr, kin, rin, kout, rout, perm, d_n, shift, bits, counts, digit_total, max_tiles);
     }
     rin = rout;
