@@ -125,23 +125,105 @@ adj_m2l_kernel(const float4* __restrict__ cell4, const float2* __restrict__ cell
   cell_g[off + ty * dim + tx] = make_float4(gx, gy, gm, 0.0f);
 }
 
+// The transposed M2L of every level with at most kAdjWideDim cells per side, in one launch: levels do not depend
+// on one another here (G of a level comes from that level's centres and Lambda). One warp per cell: lane j takes
+// candidate j of the 6 x 6 children of the parent's neighbourhood (j and j + 32 for the first four lanes), and the
+// contributions are summed by a fixed butterfly over the lanes. Cells [first_cell, lv.total) of the compact
+// layout.
+constexpr int kAdjWideDim = 128;
+
+__device__ __forceinline__ void adj_m2l_pair(const float4 C, const float2 LC, const float4 S, const float2 LS,
+                                             float eps, float& gx, float& gy, float& gm) {
+  const float dx = S.x - C.x, dy = S.y - C.y;
+  const float r2 = dx * dx + dy * dy;
+  const float r = sqrtf(r2);
+  const float inv = 1.0f / (r2 * r + eps);
+  const float ux = C.z * LS.x - S.z * LC.x;
+  const float uy = C.z * LS.y - S.z * LC.y;
+  const float k3 = 3.0f * r * inv * inv * (dx * ux + dy * uy);
+  gx += ux * inv - k3 * dx;
+  gy += uy * inv - k3 * dy;
+  gm -= (LS.x * dx + LS.y * dy) * inv;
+}
+
+__global__ void __launch_bounds__(256) adj_m2l_wide_kernel(const float4* __restrict__ cell4,
+                                                           const float2* __restrict__ cell_lam,
+                                                           float4* __restrict__ cell_g, Levels lv, int first_cell,
+                                                           float eps) {
+  const int lane = threadIdx.x & 31;
+  const int c = first_cell + (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+  if (c >= lv.total) return;  // warp-uniform
+  int l = lv.count - 1;
+  while (l > 0 && lv.offset[l] > c) --l;
+  const int dim = lv.dim[l], off = lv.offset[l];
+  const int k = c - off, tx = k % dim, ty = k / dim;
+  const float4 C = cell4[c];
+  const float2 LC = cell_lam[c];
+  const int px = tx & ~1, py = ty & ~1;
+  float gx = 0.0f, gy = 0.0f, gm = 0.0f;
+  for (int j = lane; j < 36; j += 32) {
+    const int x = px - 2 + j % 6, y = py - 2 + j / 6;
+    if (x >= 0 && x < dim && y >= 0 && y < dim && (abs(x - tx) > 1 || abs(y - ty) > 1)) {
+      adj_m2l_pair(C, LC, cell4[off + y * dim + x], cell_lam[off + y * dim + x], eps, gx, gy, gm);
+    }
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    gx += __shfl_xor_sync(0xffffffffu, gx, o);
+    gy += __shfl_xor_sync(0xffffffffu, gy, o);
+    gm += __shfl_xor_sync(0xffffffffu, gm, o);
+  }
+  if (lane == 0) cell_g[c] = make_float4(gx, gy, gm, 0.0f);
+}
+
+// Lambda up (adj_up_kernel) for levels l_from..top, then nothing else: one CTA, level after level.
+__global__ void __launch_bounds__(256) adj_up_top_kernel(float2* __restrict__ cell_lam, Levels lv, int l_from) {
+  for (int l = l_from; l < lv.count; ++l) {
+    const int dim_p = lv.dim[l], dim_c = lv.dim[l - 1], off_c = lv.offset[l - 1], off_p = lv.offset[l];
+    for (int k = threadIdx.x; k < dim_p * dim_p; k += blockDim.x) {
+      const int px = k % dim_p, py = k / dim_p;
+      const int c0 = off_c + (2 * py) * dim_c + 2 * px;
+      const float2 a = cell_lam[c0], b = cell_lam[c0 + 1], c = cell_lam[c0 + dim_c], d = cell_lam[c0 + dim_c + 1];
+      cell_lam[off_p + k] = make_float2(((a.x + b.x) + c.x) + d.x, ((a.y + b.y) + c.y) + d.y);
+    }
+    __syncthreads();
+  }
+}
+
 // Transposed M2M: a parent's G flows to its children through the centre of mass (m2m.cu:40-53).
+__device__ __forceinline__ void adj_down_child(const float4* __restrict__ cell4, float4* __restrict__ cell_g,
+                                               int off_c, int dim_c, int off_p, int dim_p, int k) {
+  const int x = k % dim_c, y = k / dim_c;
+  const int p = off_p + (y >> 1) * dim_p + (x >> 1);
+  const float4 P = cell4[p];
+  if (P.z == 0.0f) return;  // an empty parent has a fixed (0, 0) centre: nothing flows
+  const float4 GP = cell_g[p];
+  const float4 ch = cell4[off_c + k];
+  float4 g = cell_g[off_c + k];
+  const float f = ch.z / P.z;
+  g.x += f * GP.x;
+  g.y += f * GP.y;
+  g.z += GP.z + (GP.x * (ch.x - P.x) + GP.y * (ch.y - P.y)) / P.z;
+  cell_g[off_c + k] = g;
+}
+
 __global__ void adj_down_kernel(const float4* __restrict__ cell4, float4* __restrict__ cell_g, int off_c, int dim_c,
                                 int off_p, int dim_p) {
   const int total = dim_c * dim_c;
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < total; k += gridDim.x * blockDim.x) {
-    const int x = k % dim_c, y = k / dim_c;
-    const int p = off_p + (y >> 1) * dim_p + (x >> 1);
-    const float4 P = cell4[p];
-    if (P.z == 0.0f) continue;  // an empty parent has a fixed (0, 0) centre: nothing flows
-    const float4 GP = cell_g[p];
-    const float4 ch = cell4[off_c + k];
-    float4 g = cell_g[off_c + k];
-    const float f = ch.z / P.z;
-    g.x += f * GP.x;
-    g.y += f * GP.y;
-    g.z += GP.z + (GP.x * (ch.x - P.x) + GP.y * (ch.y - P.y)) / P.z;
-    cell_g[off_c + k] = g;
+    adj_down_child(cell4, cell_g, off_c, dim_c, off_p, dim_p, k);
+  }
+}
+
+// adj_down for parent levels top..l_to (children down to level l_to - 1) in one CTA, level after level.
+__global__ void __launch_bounds__(256) adj_down_top_kernel(const float4* __restrict__ cell4,
+                                                           float4* __restrict__ cell_g, Levels lv, int l_to) {
+  for (int l = lv.count - 1; l >= l_to; --l) {
+    const int dim_c = lv.dim[l - 1];
+    for (int k = threadIdx.x; k < dim_c * dim_c; k += blockDim.x) {
+      adj_down_child(cell4, cell_g, lv.offset[l - 1], dim_c, lv.offset[l], lv.dim[l], k);
+    }
+    __syncthreads();
   }
 }
 
@@ -573,18 +655,39 @@ struct nbfmm_adjoint {
     const bool far = v.geo.num_level > 0;
     if (far) {
       if (!cached) launch_m2m(v.lv, v.cell4, s);  // a cached slot holds every level
-      for (int l = 1; l < v.lv.count; ++l) {
+      // Lambda up: per level while the parents have more than kAdjSmall cells per side, then one launch.
+      constexpr int kAdjSmall = 64;
+      int l = 1;
+      for (; l < v.lv.count && v.lv.dim[l] > kAdjSmall; ++l) {
         adj_up_kernel<<<grid_for((long long)v.lv.dim[l] * v.lv.dim[l], 256, 152 * 8), 256, 0, s>>>(
             cell_lam, v.lv.offset[l - 1], v.lv.dim[l - 1], v.lv.offset[l], v.lv.dim[l]);
       }
-      for (int l = 0; l < v.lv.count; ++l) {
-        const int d = v.lv.dim[l];
-        const dim3 grid((d + kM2LTile - 1) / kM2LTile, (d + kM2LTile - 1) / kM2LTile);
-        adj_m2l_kernel<<<grid, dim3(kM2LTile, kM2LTile), 0, s>>>(v.cell4, cell_lam, cell_g, v.lv.offset[l], d, v.eps);
+      if (l < v.lv.count) adj_up_top_kernel<<<1, 256, 0, s>>>(cell_lam, v.lv, l);
+      // Transposed M2L: large levels per level, the small ones in one launch.
+      int lw = v.lv.count;
+      for (int q = 0; q < v.lv.count; ++q) {
+        if (v.lv.dim[q] <= kAdjWideDim) {
+          lw = q;
+          break;
+        }
       }
-      for (int l = v.lv.count - 1; l >= 1; --l) {
-        adj_down_kernel<<<grid_for((long long)v.lv.dim[l - 1] * v.lv.dim[l - 1], 256, 152 * 8), 256, 0, s>>>(
-            v.cell4, cell_g, v.lv.offset[l - 1], v.lv.dim[l - 1], v.lv.offset[l], v.lv.dim[l]);
+      for (int q = 0; q < lw; ++q) {
+        const int d = v.lv.dim[q];
+        const dim3 grid((d + kM2LTile - 1) / kM2LTile, (d + kM2LTile - 1) / kM2LTile);
+        adj_m2l_kernel<<<grid, dim3(kM2LTile, kM2LTile), 0, s>>>(v.cell4, cell_lam, cell_g, v.lv.offset[q], d, v.eps);
+      }
+      if (lw < v.lv.count) {
+        const long long cells_w = (long long)v.lv.total - v.lv.offset[lw];
+        adj_m2l_wide_kernel<<<(unsigned)((cells_w * 32 + 255) / 256), 256, 0, s>>>(v.cell4, cell_lam, cell_g, v.lv,
+                                                                                  v.lv.offset[lw], v.eps);
+      }
+      // G down: the small parent levels in one launch, then per level.
+      int ld = v.lv.count - 1;
+      while (ld >= 1 && v.lv.dim[ld - 1] <= kAdjSmall) --ld;  // parent levels ld+1.. have children of <= kAdjSmall
+      if (ld + 1 <= v.lv.count - 1) adj_down_top_kernel<<<1, 256, 0, s>>>(v.cell4, cell_g, v.lv, ld + 1);
+      for (int q = ld; q >= 1; --q) {
+        adj_down_kernel<<<grid_for((long long)v.lv.dim[q - 1] * v.lv.dim[q - 1], 256, 152 * 8), 256, 0, s>>>(
+            v.cell4, cell_g, v.lv.offset[q - 1], v.lv.dim[q - 1], v.lv.offset[q], v.lv.dim[q]);
       }
     }
     AdjP2PArgs a{};
