@@ -382,28 +382,39 @@ def measure_batched(steps, warmup):
     from nbfmm_gb300 import autotune, workloads
 
     sysb = workloads.batched()
-    levels, report = autotune.tune_levels(nbfmm_gb300, sysb)
+    levels, passes, report = autotune.tune(nbfmm_gb300, sysb)
+    levels_d, report_d = autotune.tune_levels(nbfmm_gb300, sysb)
     prev = sysb.previous()
     n = sysb.n
-    b = nbfmm_gb300.Batch(sysb.offsets, levels, sysb.limits, tick=sysb.dt, grav_const=sysb.grav_const,
-                          epsilon=sysb.epsilon)
-    b.position_cur[:] = torch.from_numpy(sysb.position).cuda()
-    b.position_pre[:] = torch.from_numpy(prev).cuda()
-    b.weight[:] = torch.from_numpy(sysb.weight).cuda()
-    b.update(warmup)
-    torch.cuda.synchronize()
-    b.profile_begin(steps)
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     clocks = ClockSampler("0")
-    e0.record()
-    b.update(steps)
-    e1.record()
-    torch.cuda.synchronize()
+
+    def run(lv, item_passes, profile):
+        b = nbfmm_gb300.Batch(sysb.offsets, lv, sysb.limits, tick=sysb.dt, grav_const=sysb.grav_const,
+                              epsilon=sysb.epsilon)
+        if item_passes is not None:
+            b.set_item_passes(item_passes)
+        b.position_cur[:] = torch.from_numpy(sysb.position).cuda()
+        b.position_pre[:] = torch.from_numpy(prev).cuda()
+        b.weight[:] = torch.from_numpy(sysb.weight).cuda()
+        b.update(warmup)
+        torch.cuda.synchronize()
+        if profile:
+            b.profile_begin(steps)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        b.update(steps)
+        e1.record()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)
+        p2p = b.profile_end()[0] if profile else None
+        launches = b.kernel_launches(steps)
+        b.close()
+        return ms, p2p, launches
+
+    batched_ms, p2p_ms, launches = run(levels, passes, True)
+    depth_only_ms, _, _ = run(levels_d, None, False)
     clk = clocks.stop()
-    batched_ms = e0.elapsed_time(e1)
-    p2p_ms, p2p_k = b.profile_end()
-    launches = b.kernel_launches(steps)
-    b.close()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
 
     stars = []
     for s in range(sysb.num_systems):
@@ -432,6 +443,8 @@ def measure_batched(steps, warmup):
         "config": {"workload": f"batched: {sysb.num_systems} systems, N lognormal(median 20k, sd 0.8) clipped to "
                                f"[2k, 262k], {n:,} particles, squares and disks, eps {sysb.epsilon:g}, "
                                f"dt {sysb.dt:g}", "autotune": report},
+        "depth_only_tuning": {"value": n * steps / (depth_only_ms / 1e3), "ms_per_step": depth_only_ms / steps,
+                              "how": "tree depth chosen per bucket, P2P items of 4 passes", "autotune": report_d},
         "looped": {"value": looped, "ms_per_step": looped_ms / steps,
                    "how": "one Stars per system with the same depths; update(K) per system, one after another"},
         "speedup_vs_looped": value / looped,

@@ -146,6 +146,9 @@ int nbfmm_batch_create(int num_systems, const int* particle_offsets, const int* 
 int nbfmm_batch_destroy(nbfmm_batch* batch);
 int nbfmm_batch_set_epsilon(nbfmm_batch* batch, float epsilon);
 int nbfmm_batch_set_arithmetic(nbfmm_batch* batch, int arithmetic); /* nbfmm_solver_set_arithmetic */
+/* P2P work-item size per system (host array of num_systems values, 2 or 4 passes of 32 target stars; 4 by
+ * default): a tile shape for the autotuner. Results do not depend on it. Takes effect from the next update. */
+int nbfmm_batch_set_item_passes(nbfmm_batch* batch, const int* passes_per_item);
 /* Device state arrays over all systems (float2 / float2 / float [particle_offsets[num_systems]]). */
 int nbfmm_batch_state(nbfmm_batch* batch, float** gpuptr_position_cur, float** gpuptr_position_pre,
                       float** gpuptr_weight);

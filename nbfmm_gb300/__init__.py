@@ -360,6 +360,16 @@ class Batch:
         _check(_lib.load().nbfmm_batch_set_arithmetic(self._h, _arithmetic(arithmetic)))
         self.arithmetic = arithmetic
 
+    def set_item_passes(self, passes_per_item):
+        """P2P work-item size of each system: 2 or 4 passes of 32 target stars (a tile shape; results do not
+        depend on it)."""
+        import numpy as np
+
+        p = np.ascontiguousarray(passes_per_item, dtype=np.int32)
+        if len(p) != self.num_systems:
+            raise ValueError("one value per system")
+        _check(_lib.load().nbfmm_batch_set_item_passes(self._h, p.ctypes.data_as(ctypes.POINTER(ctypes.c_int))))
+
     @property
     def position_cur(self):
         return _as_tensor(self._ptrs[0], (max(self.num_particles, 1), 2), "<f4")[: self.num_particles]

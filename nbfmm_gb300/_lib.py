@@ -62,6 +62,7 @@ SIGNATURES = {
     "nbfmm_batch_destroy": (ctypes.c_int, [_vp]),
     "nbfmm_batch_set_epsilon": (ctypes.c_int, [_vp, ctypes.c_float]),
     "nbfmm_batch_set_arithmetic": (ctypes.c_int, [_vp, ctypes.c_int]),
+    "nbfmm_batch_set_item_passes": (ctypes.c_int, [_vp, _c_int_p]),
     "nbfmm_batch_state": (ctypes.c_int, [_vp, ctypes.POINTER(_vp), ctypes.POINTER(_vp), ctypes.POINTER(_vp)]),
     "nbfmm_batch_num_stars": (ctypes.c_int, [_vp, _c_int_p]),
     "nbfmm_batch_update": (ctypes.c_int, [_vp, ctypes.c_int, _vp]),

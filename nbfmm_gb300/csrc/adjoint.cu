@@ -457,8 +457,8 @@ __global__ void __launch_bounds__(kAdjWarps * 32, 4) adj_p2p_kernel(const AdjP2P
     rg.s1 = a.head[lo + cy * B];
     rg.l1 = a.head[hi + cy * B + 1] - rg.s1;
     if (cy + 1 < B) { rg.s2 = a.head[lo + (cy + 1) * B]; rg.l2 = a.head[hi + (cy + 1) * B + 1] - rg.s2; }
-    const int first = a.head[cell] + wc.y * kP2PChunk;
-    const int last = min(first + kP2PChunk, a.head[cell + 1]);
+    const int first = a.head[cell] + item_first_pass(wc.y) * 32;
+    const int last = min(first + item_passes(wc.y) * 32, a.head[cell + 1]);
     switch ((last - first + 31) >> 5) {
       case 1: adj_item<0, 1>(a, sl, lane, cell, first, last, rg); break;
       case 2: adj_item<1, 0>(a, sl, lane, cell, first, last, rg); break;

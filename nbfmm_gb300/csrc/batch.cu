@@ -287,6 +287,7 @@ struct nbfmm_batch {
   int* levels = nullptr;
   int* level_base = nullptr;  // [max_levels][S + 1]
   int* tile_base = nullptr;   // [max_levels][S + 1]
+  int* sys_passes = nullptr;  // [S] passes of 32 targets per P2P work item of each system (2 or 4)
   // Sort, tree and P2P workspace.
   uint32_t *keys_a = nullptr, *vals_a = nullptr, *keys_b = nullptr, *vals_b = nullptr;
   uint32_t *counts = nullptr, *digit_total = nullptr;
@@ -397,6 +398,7 @@ struct nbfmm_batch {
     BATCH_TRY(balloc(&levels, (size_t)S, "levels"));
     BATCH_TRY(balloc(&level_base, h_level_base.size(), "level base"));
     BATCH_TRY(balloc(&tile_base, h_tile_base.size(), "tile base"));
+    BATCH_TRY(balloc(&sys_passes, (size_t)S, "passes per item"));
     BATCH_TRY(balloc(&keys_a, N, "keys"));
     BATCH_TRY(balloc(&vals_a, N, "values"));
     BATCH_TRY(balloc(&keys_b, N, "keys"));
@@ -422,6 +424,8 @@ struct nbfmm_batch {
     cudaMemcpy(geo, hg.data(), sizeof(Geometry) * S, cudaMemcpyHostToDevice);
     cudaMemcpy(sys_of_orig, h_sys_of_orig.data(), sizeof(int) * (size_t)n, cudaMemcpyHostToDevice);
     cudaMemcpy(cell_base, h_cell_base.data(), sizeof(int) * (S + 1), cudaMemcpyHostToDevice);
+    const std::vector<int> h_passes(S, kP2PPasses);
+    cudaMemcpy(sys_passes, h_passes.data(), sizeof(int) * S, cudaMemcpyHostToDevice);
     cudaMemcpy(part_off, h_off.data(), sizeof(int) * (S + 1), cudaMemcpyHostToDevice);
     cudaMemcpy(dim, h_dim.data(), sizeof(int) * S, cudaMemcpyHostToDevice);
     cudaMemcpy(levels, h_levels.data(), sizeof(int) * S, cudaMemcpyHostToDevice);
@@ -459,6 +463,7 @@ struct nbfmm_batch {
     if (cap_b) cudaEventDestroy(cap_b);
     if (capture_stream) cudaStreamDestroy(capture_stream);
     bfree(geo); bfree(sys_of_orig); bfree(cell_base); bfree(dim); bfree(levels); bfree(level_base); bfree(tile_base);
+    bfree(sys_passes);
     bfree(keys_a); bfree(vals_a); bfree(keys_b); bfree(vals_b); bfree(counts); bfree(digit_total);
     bfree(head); bfree(work); bfree(sorted4); bfree(sprev); bfree(cell4); bfree(ceff);
     bfree(cur); bfree(prev); bfree(w); bfree(state4); bfree(state_prev); bfree(grave); bfree(order_scratch); bfree(sys_counts);
@@ -496,7 +501,7 @@ struct nbfmm_batch {
                                                                 (uint32_t)total_leaf, keys_a, vals_a, grave);
     sort(sc.n_cur, key_bits, s);
     launch_head(skey, sc.n_cur, total_leaf, head, sc.n_alive, s);
-    launch_worklist(head, total_leaf, work, d_work_count(), true, s);
+    launch_worklist(head, total_leaf, work, d_work_count(), true, s, kP2PPasses, cell_base, sys_passes, S);
     // gather + P2M over the global leaf space, each cell in index order
     launch_gather_state_ordered(head, total_leaf, perm, state4, state_prev, sorted4, sprev, cell4, order_scratch, N, s);
     for (int lv = 1; lv < max_levels; ++lv) {
@@ -666,6 +671,25 @@ int nbfmm_batch_set_arithmetic(nbfmm_batch* batch, int arithmetic) {
   }
   batch->drop_graph();
   batch->exact = arithmetic;
+  return NBFMM_OK;
+}
+
+int nbfmm_batch_set_item_passes(nbfmm_batch* batch, const int* passes_per_item) {
+  if (!batch) return api_fail(NBFMM_ERR_INVALID, "null batch handle");
+  if (!passes_per_item) return api_fail(NBFMM_ERR_INVALID, "null table");
+  for (int s = 0; s < batch->S; ++s) {
+    if (passes_per_item[s] != 2 && passes_per_item[s] != 4) {
+      return api_fail(NBFMM_ERR_INVALID, "passes per item of system %d must be 2 or 4, got %d", s, passes_per_item[s]);
+    }
+  }
+  if (batch->S > 0) {
+    const cudaError_t e = cudaMemcpy(batch->sys_passes, passes_per_item, sizeof(int) * batch->S,
+                                     cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      return api_fail(NBFMM_ERR_CUDA, "nbfmm_batch_set_item_passes: %s", cudaGetErrorString(e));
+    }
+  }
   return NBFMM_OK;
 }
 

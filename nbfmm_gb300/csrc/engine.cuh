@@ -29,11 +29,18 @@ constexpr int kRecItems = 16;            // record sort: items per thread
 constexpr int kRecTile = kSortThreads * kRecItems;  // 4096 items per tile
 constexpr int kP2PThreads = 128;        // 4 independent warps per CTA
 constexpr int kP2PPasses = 4;            // targets per lane in one work item (4 passes of 32)
-constexpr int kP2PChunk = 32 * kP2PPasses;  // targets per work item
+constexpr int kP2PChunk = 32 * kP2PPasses;  // targets per work item, by default
+constexpr int kP2PMinChunk = 64;             // the smallest work item a work list may use (2 passes)
 
-// Work list entries a solve may need: a non-empty cell of n targets yields at most n/kP2PChunk + 2 items
-// (its chunks and one paired-tail item) with paired tails, at most n/kP2PChunk + 1 without.
-inline size_t work_list_capacity(size_t num_cells, size_t n) { return 2 * num_cells + n / kP2PChunk + 1; }
+// A P2P work item is (cell, y). y >= 0: the item runs passes [first, first + passes) of 32 targets of the cell,
+// encoded first | passes << 24 (passes 1..4); y = -1: the paired tails of the cell and the next (launch_worklist).
+__host__ __device__ __forceinline__ int work_item(int first_pass, int passes) { return first_pass | (passes << 24); }
+__host__ __device__ __forceinline__ int item_first_pass(int y) { return y & 0xFFFFFF; }
+__host__ __device__ __forceinline__ int item_passes(int y) { return y >> 24; }
+
+// Work list entries a solve may need: a non-empty cell of n targets yields at most n/kP2PMinChunk + 2 items
+// (its chunks and one paired-tail item) with paired tails, at most n/kP2PMinChunk + 1 without.
+inline size_t work_list_capacity(size_t num_cells, size_t n) { return 2 * num_cells + n / kP2PMinChunk + 1; }
 
 #ifndef NBFMM_P2P_PAIR_TAILS
 #define NBFMM_P2P_PAIR_TAILS 1  // 0: never pair tails, whatever a launch asks
@@ -198,15 +205,19 @@ void launch_head(const uint32_t* keys, const int* d_n, int num_cells, int* head,
                  cudaStream_t stream);
 
 // Work list of (cell, chunk) items over non-empty leaf cells; *d_work_count receives the count.
-// Work items of the non-empty cells: (cell, k) covers the cell's targets [128k, 128k + 128). With pair_tails, a
-// cell whose tail is paired (tails_paired) clips its chunks to its whole passes of 32 targets, and the even
-// cell of the pair files one more item, (cell, -1): the tails of cell and cell + 1. p2p_kernel reads both
-// layouts (P2PArgs::pair_tails). Measured on GB300: pairing takes 1.4% off P2P on a 16.8M two-disk step and 5%
-// off 20k-star steps, and costs 5% on the batched form's launch of 512 small systems. The batched form pairs
+// Work items of the non-empty cells: a cell's passes of 32 targets in items of `passes_per_item` passes (2 or 4;
+// with sys_passes, the value of the cell's system, found by binary search over sys_cell_base[0..num_systems]).
+// With pair_tails, a cell whose tail is paired (tails_paired) clips its items to its whole passes of 32 targets,
+// and the even cell of the pair files one more item, (cell, -1): the tails of cell and cell + 1. p2p_kernel reads
+// both layouts (P2PArgs::pair_tails). Measured on GB300: pairing takes 1.4% off P2P on a 16.8M two-disk step and
+// 5% off 20k-star steps, and costs 5% on the batched form's launch of 512 small systems. The batched form pairs
 // all the same: which sources take the Newton reciprocal follows their place in a pass, so a batched system
-// stays bit-identical to the same system stepped alone only if both pair alike.
+// stays bit-identical to the same system stepped alone only if both pair alike. The item size does not change
+// any result: a pass is packed with the same neighbour pass (0-1, 2-3) and a cell's odd last pass runs alone
+// whether items hold 2 or 4 passes.
 void launch_worklist(const int* head, int num_cells, int2* work, int* d_work_count, bool pair_tails,
-                     cudaStream_t stream);
+                     cudaStream_t stream, int passes_per_item = kP2PPasses, const int* sys_cell_base = nullptr,
+                     const int* sys_passes = nullptr, int num_systems = 0);
 
 // P2M on the sorted particles: leaf centres of mass summed in sorted order (predo, and the stage entry point).
 void launch_p2m(const Geometry& g, const int* head, const float4* sorted4, float4* cell0, cudaStream_t stream);

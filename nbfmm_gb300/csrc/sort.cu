@@ -387,16 +387,27 @@ __global__ void head_kernel(const uint32_t* __restrict__ keys, const int* __rest
 }
 
 __global__ void worklist_kernel(const int* __restrict__ head, int num_cells, int2* __restrict__ work,
-                                int* __restrict__ d_work_count, int pair_tails) {
+                                int* __restrict__ d_work_count, int pair_tails, int passes_per_item,
+                                const int* __restrict__ sys_cell_base, const int* __restrict__ sys_passes,
+                                int num_systems) {
   const int lane = threadIdx.x & 31;
   // Whole warps iterate together so that the warp-wide scan below sees every lane.
   for (int base = blockIdx.x * blockDim.x; base < num_cells; base += gridDim.x * blockDim.x) {
     const int c = base + threadIdx.x;
-    int chunks = 0, tails = 0;
+    int chunks = 0, tails = 0, ppi = passes_per_item, passes = 0;
     if (c < num_cells) {
+      if (sys_passes) {  // the cell's system: the last whose first cell is <= c
+        int lo = 0, hi = num_systems;
+        while (hi - lo > 1) {
+          const int mid = (lo + hi) >> 1;
+          if (sys_cell_base[mid] <= c) lo = mid; else hi = mid;
+        }
+        ppi = sys_passes[lo];
+      }
       const int nt = head[c + 1] - head[c];
       const bool paired = pair_tails && tails_paired(head, c);
-      chunks = ((paired ? nt & ~31 : nt) + kP2PChunk - 1) / kP2PChunk;
+      passes = ((paired ? nt & ~31 : nt) + 31) >> 5;
+      chunks = (passes + ppi - 1) / ppi;
       tails = (paired && !(c & 1)) ? 1 : 0;  // the even cell files the pair
     }
     const int items = chunks + tails;
@@ -410,7 +421,7 @@ __global__ void worklist_kernel(const int* __restrict__ head, int num_cells, int
     if (lane == 31 && incl > 0) start = atomicAdd(d_work_count, incl);
     start = __shfl_sync(0xffffffffu, start, 31);
     int2* out = work + start + incl - items;
-    for (int k = 0; k < chunks; ++k) out[k] = make_int2(c, k);
+    for (int k = 0; k < chunks; ++k) out[k] = make_int2(c, work_item(k * ppi, min(ppi, passes - k * ppi)));
     if (tails) out[chunks] = make_int2(c, -1);
   }
 }
@@ -522,10 +533,12 @@ void launch_head(const uint32_t* keys, const int* d_n, int num_cells, int* head,
 }
 
 void launch_worklist(const int* head, int num_cells, int2* work, int* d_work_count, bool pair_tails,
-                     cudaStream_t stream) {
+                     cudaStream_t stream, int passes_per_item, const int* sys_cell_base, const int* sys_passes,
+                     int num_systems) {
   cudaMemsetAsync(d_work_count, 0, sizeof(int), stream);
-  worklist_kernel<<<grid_for(num_cells, 256, 152 * 8), 256, 0, stream>>>(head, num_cells, work, d_work_count,
-                                                                        pair_tails ? 1 : 0);
+  worklist_kernel<<<grid_for(num_cells, 256, 152 * 8), 256, 0, stream>>>(
+      head, num_cells, work, d_work_count, pair_tails ? 1 : 0, passes_per_item, sys_cell_base, sys_passes,
+      num_systems);
 }
 
 void launch_keys_from_head(const int* head, int num_cells, uint32_t* skey, cudaStream_t stream) {

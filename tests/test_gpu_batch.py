@@ -49,12 +49,14 @@ def run_alone(engine, cur, prev, w, level, lim, tick, eps, calls):
         st.gpuptr_weight_.cpu().numpy()
 
 
-def run_batch(engine, systems, tick, eps, calls, arithmetic="fast"):
+def run_batch(engine, systems, tick, eps, calls, arithmetic="fast", item_passes=None):
     import torch
 
     offsets = np.cumsum([0] + [len(s[2]) for s in systems])
     b = engine.Batch(offsets, [s[3] for s in systems], [s[4] for s in systems], tick=tick, epsilon=eps,
                      arithmetic=arithmetic)
+    if item_passes is not None:
+        b.set_item_passes(item_passes)
     b.position_cur[:] = torch.from_numpy(np.concatenate([s[0] for s in systems])).cuda()
     b.position_pre[:] = torch.from_numpy(np.concatenate([s[1] for s in systems])).cuda()
     b.weight[:] = torch.from_numpy(np.concatenate([s[2] for s in systems])).cuda()
@@ -64,11 +66,14 @@ def run_batch(engine, systems, tick, eps, calls, arithmetic="fast"):
     return b, offsets
 
 
-@pytest.mark.parametrize("calls", [[1], [5], [2, 3]])
-def test_batch_equals_systems_alone(engine, calls):
+@pytest.mark.parametrize("calls,item_passes", [([1], None), ([5], None), ([2, 3], None),
+                                               ([3], [2, 4, 2, 2, 4, 2])])
+def test_batch_equals_systems_alone(engine, calls, item_passes):
+    """Each system of a batch evolves bit for bit as the same system in a Stars of its own; with P2P work items of
+    2 passes for some systems (the autotuner's tile choice) as well, which must not change any result."""
     systems = make_systems(7)
     tick, eps = 2e-3, 1e-3
-    b, off = run_batch(engine, systems, tick, eps, calls)
+    b, off = run_batch(engine, systems, tick, eps, calls, item_passes=item_passes)
     cur = b.position_cur.cpu().numpy()
     pre = b.position_pre.cpu().numpy()
     w = b.weight.cpu().numpy()
@@ -103,6 +108,15 @@ def test_exact_arithmetic_batch_equals_the_oracle(engine, orc):
         np.testing.assert_array_equal(w[sl], ww)
         np.testing.assert_array_equal(cur[sl], c)
         np.testing.assert_array_equal(pre[sl], p)
+
+
+def test_item_passes_must_be_two_or_four(engine):
+    systems = make_systems(8)
+    b, _ = run_batch(engine, systems, 1e-3, 1e-3, [])
+    with pytest.raises(engine.NbfmmError):
+        b.set_item_passes([3] * len(systems))
+    with pytest.raises(ValueError):
+        b.set_item_passes([2])
 
 
 def test_batch_launch_count_and_profile(engine):
