@@ -647,7 +647,7 @@ struct nbfmm_adjoint {
   // work list is rebuilt (the solve's pairs tails; adj_p2p_kernel reads plain 128-target chunks).
   void vjp(const float2* pos, const float2* lam, float scale, bool cached, cudaStream_t s) {
     nbfmm_solver& v = *solver;
-    if (cached) launch_worklist(v.head, v.num_cells, v.work, v.d_work_count(), false, s);
+    if (cached) launch_worklist(v.head, v.num_cells, v.work, v.d_work_count(), false, s, v.item_passes);
     else v.predo(n, pos, m, s, false);
     const int cells = v.num_cells;
     adj_gather_kernel<<<grid_for((long long)cells * 32, 256, 152 * 16), 256, 0, s>>>(cells, v.head, v.perm, lam,

@@ -161,7 +161,8 @@ int nbfmm_solver_p2p(nbfmm_solver* solver, int num_particle, void* stream) {
   NBFMM_TRY(check_solver(solver));
   NBFMM_TRY(check_n(solver, num_particle));
   cudaStream_t s = as_stream(stream);
-  launch_worklist(solver->head, solver->num_cells, solver->work, solver->d_work_count(), true, s);
+  launch_worklist(solver->head, solver->num_cells, solver->work, solver->d_work_count(), true, s,
+                  solver->item_passes);
   P2PArgs a = solver->p2p_args();
   a.seff = solver->seff;
   launch_p2p(a, kStoreSorted, solver->num_sms, s);
@@ -342,7 +343,7 @@ struct nbfmm_stars {
     launch_keys_from_state(v.geo, sc, state4, state_prev, dead, v.keys_a, v.vals_a, grave, max_n, s);
     v.sort(sc.n_cur, v.key_bits, s);
     launch_head(v.skey, sc.n_cur, v.num_cells, v.head, sc.n_alive, s);
-    launch_worklist(v.head, v.num_cells, v.work, v.d_work_count(), true, s);
+    launch_worklist(v.head, v.num_cells, v.work, v.d_work_count(), true, s, v.item_passes);
     launch_gather_state_ordered(v.head, v.num_cells, v.perm, state4, state_prev, v.sorted4, sprev, v.cell0(),
                                 order_scratch, max_n, s);  // each cell in index order, as the reference sorts
     v.far_field(s);

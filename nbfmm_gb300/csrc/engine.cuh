@@ -28,7 +28,10 @@ constexpr int kRecMaxBits = 10;          // digit bits per pass of the record so
 constexpr int kRecItems = 16;            // record sort: items per thread
 constexpr int kRecTile = kSortThreads * kRecItems;  // 4096 items per tile
 constexpr int kP2PThreads = 128;        // 4 independent warps per CTA
-constexpr int kP2PPasses = 4;            // targets per lane in one work item (4 passes of 32)
+#ifndef NBFMM_P2P_ITEM_PASSES
+#define NBFMM_P2P_ITEM_PASSES 4
+#endif
+constexpr int kP2PPasses = NBFMM_P2P_ITEM_PASSES;  // passes of 32 targets in one work item, by default (2 or 4)
 constexpr int kP2PChunk = 32 * kP2PPasses;  // targets per work item, by default
 constexpr int kP2PMinChunk = 64;             // the smallest work item a work list may use (2 passes)
 
