@@ -352,6 +352,12 @@ struct nbfmm_stars {
     a.state4 = state4;
     a.state_prev = state_prev;
     a.tick = tick;
+    a.grave = grave;
+    a.d_step = sc.step;
+    a.d_num_steps = sc.num_steps;
+    a.d_sort_n = sc.sort_n;
+    a.d_n_import = sc.n_import;
+    a.lim = make_float4(v.geo.xmin, v.geo.ymin, v.geo.xmax, v.geo.ymax);
     // External records: captured as event record nodes (a plain record is only a capture-ordering marker).
     cudaEventRecordWithFlags(cap_a, s, cudaEventRecordExternal);
     launch_p2p(a, kVerlet, v.num_sms, s);
@@ -429,7 +435,7 @@ struct nbfmm_stars {
     // most recent first (fate 1, 2, ...), each group in original order.
     // When the call lost no star (sort_n == 0) the fate keys, the sort and the head run over nothing and the
     // export is the identity.
-    launch_export_fate(v.geo, sc, state4, state_prev, grave, max_n, s);
+    launch_export_fate(sc, s);
     launch_fate_keys(sc, grave, v.keys_a, v.vals_a, max_n, s);
     v.sort(sc.sort_n, fate_bits(steps), s);
     launch_head(v.skey, sc.sort_n, 1, v.head, sc.num_star, s);  // head[1] = number of fate-0 stars

@@ -267,6 +267,13 @@ struct P2PArgs {
   float4* state4;          // kVerlet: new state (x', y', m, original index)
   float2* state_prev;      // kVerlet: new previous positions
   float tick;              // kVerlet: tick * sqrt(G)
+  // kVerlet, Stars: the final states filed on the last step of an update call (stars.cuh file_grave); null for none.
+  float4* grave;
+  const int* d_step;       // 1-based step of the call, and the call's step count
+  const int* d_num_steps;
+  int* d_sort_n;           // set to *d_n_import when a star leaves in the final prune
+  const int* d_n_import;
+  float4 lim;              // position limits (x_min, y_min, x_max, y_max) of the final prune
   // Several systems in one global leaf-cell space (batched form); num_systems == 0 for a single system.
   int num_systems;
   const int* sys_cell_base;  // [num_systems + 1] first global leaf cell of each system

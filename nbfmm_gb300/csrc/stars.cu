@@ -93,20 +93,12 @@ __global__ void finish_step_kernel(StepCounters sc) {
   *sc.prune = 1;
 }
 
-// The last prune of the call (prune.cu:40-41 on the final positions), and every star's final state filed by
-// original index: fate 0 = alive, fate 1 = pruned by the last step.
-__global__ void export_fate_kernel(Geometry g, StepCounters sc, const float4* __restrict__ state4,
-                                   const float2* __restrict__ state_prev, float4* __restrict__ grave) {
-  const int n = *sc.n_cur;
-  const int n0 = *sc.n_import;
-  // A star lost by a step or by this prune means the public order needs the fate sort.
-  if (sc.sort_n && blockIdx.x == 0 && threadIdx.x == 0 && n != n0) *sc.sort_n = n0;
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-    const float4 p = state4[i];
-    const int fate = outside(g, p.x, p.y) ? 1 : 0;
-    file_grave(grave, __float_as_int(p.w), p.x, p.y, state_prev[i], p.z, fate);
-    if (fate && sc.sort_n) *sc.sort_n = n0;
-  }
+// The last prune of the call (prune.cu:40-41 on the final positions) and every star's final state filed by
+// original index (fate 0 = alive, fate 1 = pruned by the last step) are done by the last step's P2P epilogue
+// (p2p.cu); here only a star lost by an earlier step of the call is noted: the public order then needs the fate
+// sort.
+__global__ void export_fate_kernel(StepCounters sc) {
+  if (sc.sort_n && *sc.n_cur != *sc.n_import) *sc.sort_n = *sc.n_import;
 }
 
 __global__ void fate_keys_kernel(StepCounters sc, const float4* __restrict__ grave, uint32_t* __restrict__ keys,
@@ -566,10 +558,7 @@ void launch_keys_from_state(const Geometry& g, const StepCounters& sc, const flo
 
 void launch_finish_step(const StepCounters& sc, cudaStream_t stream) { finish_step_kernel<<<1, 1, 0, stream>>>(sc); }
 
-void launch_export_fate(const Geometry& g, const StepCounters& sc, const float4* state4, const float2* state_prev,
-                        float4* grave, int max_n, cudaStream_t stream) {
-  export_fate_kernel<<<grid_for(max_n, 256, 152 * 16), 256, 0, stream>>>(g, sc, state4, state_prev, grave);
-}
+void launch_export_fate(const StepCounters& sc, cudaStream_t stream) { export_fate_kernel<<<1, 1, 0, stream>>>(sc); }
 
 void launch_fate_keys(const StepCounters& sc, const float4* grave, uint32_t* keys, uint32_t* vals, int max_n,
                       cudaStream_t stream) {

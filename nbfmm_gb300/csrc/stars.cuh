@@ -45,8 +45,9 @@ void launch_keys_from_state(const Geometry& g, const StepCounters& sc, const flo
                             uint32_t dead_key, uint32_t* keys, uint32_t* vals, float4* grave, int max_n,
                             cudaStream_t stream);
 void launch_finish_step(const StepCounters& sc, cudaStream_t stream);
-void launch_export_fate(const Geometry& g, const StepCounters& sc, const float4* state4, const float2* state_prev,
-                        float4* grave, int max_n, cudaStream_t stream);
+// After the last step of an update call: notes a star lost by a step (the last step's P2P epilogue filed every
+// remaining star's final state, P2PArgs::grave).
+void launch_export_fate(const StepCounters& sc, cudaStream_t stream);
 void launch_fate_keys(const StepCounters& sc, const float4* grave, uint32_t* keys, uint32_t* vals, int max_n,
                       cudaStream_t stream);
 // Public arrays from the records: entry i = record order[i], or record i where `sort_n` is given and holds 0
