@@ -261,15 +261,29 @@ struct nbfmm_stars {
   float4* grave = nullptr;  // final states by original index: two float4 per star (stars.cuh file_grave)
   float4* prune_rec = nullptr;  // prune()'s records, same layout
   uint32_t* order_scratch = nullptr;  // gather_state_ordered_kernel's scratch for large cells
+  // The re-sort of the steps after a call's first (stars.cuh ResortArrays).
+  uint32_t* step_key = nullptr;
+  uint32_t* step_perm = nullptr;
+  int* head_old = nullptr;
+  int* stay = nullptr;
+  int* imm_cnt = nullptr;
+  int* imm_next = nullptr;
+  int* tile_sum = nullptr;
   int* counters = nullptr;
   StepCounters sc{};
   cudaStream_t capture_stream = nullptr;
-  cudaGraph_t step_graph_def = nullptr;
-  cudaGraphExec_t step_graph = nullptr;
-  // Event record nodes around P2P in the step graph, and the profiling session's events.
+  // A call's first step sorts the imported (or resumed) state in full; the steps after it re-sort from the
+  // previous step's cell order. Each graph has event record nodes around P2P.
+  struct StepGraph {
+    cudaGraph_t def = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    cudaGraphNode_t node_a = nullptr, node_b = nullptr;
+    int kernels = 0;
+  };
+  StepGraph first_step, next_step;
+  bool graphs_built = false;
+  // The profiling session's events.
   cudaEvent_t cap_a = nullptr, cap_b = nullptr;
-  cudaGraphNode_t node_a = nullptr, node_b = nullptr;
-  int kernels_per_step = 0;
   std::vector<cudaEvent_t> prof_events;
   int prof_max = 0, prof_used = 0;
 
@@ -287,6 +301,16 @@ struct nbfmm_stars {
     NBFMM_TRY(dalloc(&grave, 2 * n, "final states"));
     NBFMM_TRY(dalloc(&prune_rec, 2 * n, "prune records"));
     NBFMM_TRY(dalloc(&order_scratch, kOrderScratch * n, "cell order scratch"));
+    const size_t cells = (size_t)solver->num_cells;
+    NBFMM_TRY(dalloc(&step_key, n, "step keys"));
+    NBFMM_TRY(dalloc(&step_perm, n, "step order"));
+    NBFMM_TRY(dalloc(&head_old, cells + 1, "previous heads"));
+    NBFMM_TRY(dalloc(&stay, cells, "stayers"));
+    NBFMM_TRY(dalloc(&imm_cnt, cells, "immigrants"));
+    NBFMM_TRY(dalloc(&imm_next, cells, "immigrant places"));
+    NBFMM_TRY(dalloc(&tile_sum, (size_t)resort_tiles(solver->num_cells), "re-sort tiles"));
+    cudaMemset(imm_cnt, 0, cells * sizeof(int));
+    cudaMemset(stay, 0, cells * sizeof(int));
     NBFMM_TRY(dalloc(&counters, 16, "step counters"));
     cudaMemset(cur, 0, n * sizeof(float2));
     cudaMemset(prev, 0, n * sizeof(float2));
@@ -310,12 +334,21 @@ struct nbfmm_stars {
     return cudaDeviceSynchronize() == cudaSuccess ? NBFMM_OK : cuda_check("stars init sync");
   }
 
+  static void drop(StepGraph& g) {
+    if (g.exec) cudaGraphExecDestroy(g.exec);
+    if (g.def) cudaGraphDestroy(g.def);
+    g = StepGraph{};
+  }
+
   void drop_graph() {
-    if (step_graph) cudaGraphExecDestroy(step_graph);
-    if (step_graph_def) cudaGraphDestroy(step_graph_def);
-    step_graph = nullptr;
-    step_graph_def = nullptr;
-    node_a = node_b = nullptr;
+    drop(first_step);
+    drop(next_step);
+    graphs_built = false;
+  }
+
+  void set_events(StepGraph& g, cudaEvent_t a, cudaEvent_t b) {
+    cudaGraphExecEventRecordNodeSetEvent(g.exec, g.node_a, a);
+    cudaGraphExecEventRecordNodeSetEvent(g.exec, g.node_b, b);
   }
 
   void drop_profile_events() {
@@ -332,19 +365,31 @@ struct nbfmm_stars {
     if (capture_stream) cudaStreamDestroy(capture_stream);
     dfree(cur); dfree(prev); dfree(w); dfree(state4); dfree(state_prev); dfree(sprev);
     dfree(grave); dfree(prune_rec); dfree(order_scratch); dfree(counters);
+    dfree(step_key); dfree(step_perm); dfree(head_old); dfree(stay); dfree(imm_cnt); dfree(imm_next);
+    dfree(tile_sum);
     delete solver;
   }
 
-  // One step: keys (with the prune of the previous step), sort, head, gather + P2M, far field,
+  // One step: the cell order (the first step of a call: keys, sort and head; a later step: the re-sort from the
+  // previous step's order, whose P2P left the keys and did the prune), the work list, gather + P2M, far field,
   // P2P + L2P + Verlet into the state, counters.
-  void enqueue_step(cudaStream_t s) {
+  void enqueue_step(cudaStream_t s, bool continuing) {
     nbfmm_solver& v = *solver;
-    const uint32_t dead = (uint32_t)v.num_cells;
-    launch_keys_from_state(v.geo, sc, state4, state_prev, dead, v.keys_a, v.vals_a, grave, max_n, s);
-    v.sort(sc.n_cur, v.key_bits, s);
-    launch_head(v.skey, sc.n_cur, v.num_cells, v.head, sc.n_alive, s);
-    launch_worklist(v.head, v.num_cells, v.work, v.d_work_count(), true, s, v.item_passes);
-    launch_gather_state_ordered(v.head, v.num_cells, v.perm, state4, state_prev, v.sorted4, sprev, v.cell0(),
+    const uint32_t* perm = nullptr;
+    if (!continuing) {
+      const uint32_t dead = (uint32_t)v.num_cells;
+      launch_keys_from_state(v.geo, sc, state4, state_prev, dead, v.keys_a, v.vals_a, grave, max_n, s);
+      v.sort(sc.n_cur, v.key_bits, s);
+      launch_head(v.skey, sc.n_cur, v.num_cells, v.head, sc.n_alive, s);
+      perm = v.perm;
+    } else {
+      ResortArrays r{head_old, step_key, stay, imm_cnt, imm_next, tile_sum, step_perm};
+      launch_resort(r, v.num_cells, max_n, v.head, sc.n_alive, s);
+      perm = step_perm;
+    }
+    launch_worklist(v.head, v.num_cells, v.work, v.d_work_count(), true, s, v.item_passes, nullptr, nullptr, 0,
+                    head_old);
+    launch_gather_state_ordered(v.head, v.num_cells, perm, state4, state_prev, v.sorted4, sprev, v.cell0(),
                                 order_scratch, max_n, s);  // each cell in index order, as the reference sorts
     v.far_field(s);
     P2PArgs a = v.p2p_args();
@@ -357,7 +402,11 @@ struct nbfmm_stars {
     a.d_num_steps = sc.num_steps;
     a.d_sort_n = sc.sort_n;
     a.d_n_import = sc.n_import;
-    a.lim = make_float4(v.geo.xmin, v.geo.ymin, v.geo.xmax, v.geo.ymax);
+    a.next_key = step_key;
+    a.next_stay = stay;
+    a.next_imm = imm_cnt;
+    a.geo = v.geo;
+    a.inv_cell = make_float2(1.0f / v.geo.cell_x, 1.0f / v.geo.cell_y);
     // External records: captured as event record nodes (a plain record is only a capture-ordering marker).
     cudaEventRecordWithFlags(cap_a, s, cudaEventRecordExternal);
     launch_p2p(a, kVerlet, v.num_sms, s);
@@ -365,43 +414,55 @@ struct nbfmm_stars {
     launch_finish_step(sc, s);
   }
 
-  int build_graph() {
+  int build_graph(StepGraph& out, bool continuing) {
     cudaGraph_t g = nullptr;
     if (cudaStreamBeginCapture(capture_stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
       return cuda_check("cudaStreamBeginCapture");
     }
-    enqueue_step(capture_stream);
+    enqueue_step(capture_stream, continuing);
     const cudaError_t e = cudaStreamEndCapture(capture_stream, &g);
     if (e != cudaSuccess) {
       cudaGetLastError();
       return fail(NBFMM_ERR_CUDA, "step capture: %s", cudaGetErrorString(e));
     }
-    const cudaError_t e2 = cudaGraphInstantiate(&step_graph, g, 0);
+    const cudaError_t e2 = cudaGraphInstantiate(&out.exec, g, 0);
     if (e2 != cudaSuccess) {
       cudaGetLastError();
       cudaGraphDestroy(g);
-      step_graph = nullptr;
+      out.exec = nullptr;
       return fail(NBFMM_ERR_CUDA, "step graph instantiate: %s", cudaGetErrorString(e2));
     }
-    step_graph_def = g;
+    out.def = g;
     size_t count = 0;
     cudaGraphGetNodes(g, nullptr, &count);
     std::vector<cudaGraphNode_t> nodes(count);
     cudaGraphGetNodes(g, nodes.data(), &count);
-    kernels_per_step = 0;
+    out.kernels = 0;
     for (cudaGraphNode_t nd : nodes) {
       cudaGraphNodeType type;
       cudaGraphNodeGetType(nd, &type);
-      if (type == cudaGraphNodeTypeKernel) ++kernels_per_step;
+      if (type == cudaGraphNodeTypeKernel) ++out.kernels;
       if (type == cudaGraphNodeTypeEventRecord) {
         cudaEvent_t ev = nullptr;
         cudaGraphEventRecordNodeGetEvent(nd, &ev);
-        if (ev == cap_a) node_a = nd;
-        if (ev == cap_b) node_b = nd;
+        if (ev == cap_a) out.node_a = nd;
+        if (ev == cap_b) out.node_b = nd;
       }
     }
-    if (!node_a || !node_b) return fail(NBFMM_ERR_CUDA, "step graph: P2P event nodes not found");
+    if (!out.node_a || !out.node_b) return fail(NBFMM_ERR_CUDA, "step graph: P2P event nodes not found");
     return cuda_check("step graph inspection");
+  }
+
+  int build_graphs() {
+    if (graphs_built) return NBFMM_OK;
+    const int rc = build_graph(first_step, false);
+    const int rc2 = rc == NBFMM_OK ? build_graph(next_step, true) : rc;
+    if (rc2 != NBFMM_OK) {
+      drop_graph();
+      return rc2;
+    }
+    graphs_built = true;
+    return NBFMM_OK;
   }
 
   // Kernels outside the step graph per update call: import, step count, and the final prune/reorder.
@@ -414,22 +475,22 @@ struct nbfmm_stars {
 
   int update(int steps, cudaStream_t s) {
     if (steps <= 0) return NBFMM_OK;
-    if (!step_graph) NBFMM_TRY(build_graph());
+    NBFMM_TRY(build_graphs());
     nbfmm_solver& v = *solver;
     launch_resume_check(sc, cur, prev, w, grave, max_n, s);
     launch_import(sc, cur, prev, w, state4, state_prev, max_n, s);
     launch_set_int(sc.num_steps, steps, s);
     for (int k = 0; k < steps; ++k) {
+      StepGraph& g = k == 0 ? first_step : next_step;
       if (prof_used < prof_max) {  // point the P2P event nodes at this step's pair
-        cudaGraphExecEventRecordNodeSetEvent(step_graph, node_a, prof_events[2 * prof_used]);
-        cudaGraphExecEventRecordNodeSetEvent(step_graph, node_b, prof_events[2 * prof_used + 1]);
+        set_events(g, prof_events[2 * prof_used], prof_events[2 * prof_used + 1]);
         ++prof_used;
       } else if (prof_max > 0 && prof_used == prof_max) {
-        cudaGraphExecEventRecordNodeSetEvent(step_graph, node_a, cap_a);
-        cudaGraphExecEventRecordNodeSetEvent(step_graph, node_b, cap_b);
+        set_events(first_step, cap_a, cap_b);
+        set_events(next_step, cap_a, cap_b);
         ++prof_used;
       }
-      if (cudaGraphLaunch(step_graph, s) != cudaSuccess) return cuda_check("cudaGraphLaunch");
+      if (cudaGraphLaunch(g.exec, s) != cudaSuccess) return cuda_check("cudaGraphLaunch");
     }
     // Final prune and the reference's order: survivors (fate 0) in original order, then the pruned stars,
     // most recent first (fate 1, 2, ...), each group in original order.
@@ -588,7 +649,7 @@ int nbfmm_stars_display(nbfmm_stars* stars, int width, int height, float size_sc
 int nbfmm_stars_profile_begin(nbfmm_stars* stars, int max_steps) {
   if (!stars) return fail(NBFMM_ERR_INVALID, "null stars handle");
   if (max_steps < 0) return fail(NBFMM_ERR_INVALID, "max_steps must be >= 0");
-  if (!stars->step_graph) NBFMM_TRY(stars->build_graph());
+  NBFMM_TRY(stars->build_graphs());
   stars->drop_profile_events();
   stars->prof_events.resize(2 * (size_t)max_steps, nullptr);
   for (auto& e : stars->prof_events) {
@@ -611,9 +672,9 @@ int nbfmm_stars_profile_end(nbfmm_stars* stars, float* p2p_ms_total, int* p2p_la
     }
     total += ms;
   }
-  if (stars->step_graph && stars->node_a) {
-    cudaGraphExecEventRecordNodeSetEvent(stars->step_graph, stars->node_a, stars->cap_a);
-    cudaGraphExecEventRecordNodeSetEvent(stars->step_graph, stars->node_b, stars->cap_b);
+  if (stars->graphs_built) {
+    stars->set_events(stars->first_step, stars->cap_a, stars->cap_b);
+    stars->set_events(stars->next_step, stars->cap_a, stars->cap_b);
   }
   stars->drop_profile_events();
   *p2p_ms_total = total;
@@ -627,10 +688,10 @@ int nbfmm_stars_kernel_launches(nbfmm_stars* stars, int num_steps, long long* la
     *launches = 0;
     return NBFMM_OK;
   }
-  if (!stars->step_graph) NBFMM_TRY(stars->build_graph());
+  NBFMM_TRY(stars->build_graphs());
   const int outside = 3 /* resume check, import, step count */ + 2 /* export fate, fate keys */ +
                       3 * stars->sort_passes(nbfmm_stars::fate_bits(num_steps)) + 1 /* head */ + 1 /* gather */;
-  *launches = (long long)num_steps * stars->kernels_per_step + outside;
+  *launches = stars->first_step.kernels + (long long)(num_steps - 1) * stars->next_step.kernels + outside;
   return NBFMM_OK;
 }
 

@@ -89,6 +89,26 @@ __device__ __forceinline__ uint32_t leaf_key(const Geometry& g, float x, float y
   return (uint32_t)(ix + iy * g.base_dim);
 }
 
+// leaf_key by a multiplication with inv = RN(1/cell): RN(d * inv) is within 1.6 * 2^-23 relative of the correctly
+// rounded quotient RN(d / cell) (two roundings of 2^-24 each, plus RN's own), so where the floors of q -/+ 2^-20 |q|
+// agree they are the floor of RN(d / cell); near a cell edge (and for NaN or infinities) the IEEE division decides.
+__device__ __forceinline__ int cell_coord_mul(float v, float lo, float cell, float inv, int dim) {
+  const float d = __fsub_rn(v, lo);
+  const float q = __fmul_rn(d, inv);
+  const float m = __fmul_rn(fabsf(q), 0x1p-20f);
+  float f = floorf(__fsub_rn(q, m));
+  if (!(f == floorf(__fadd_rn(q, m)))) f = floorf(__fdiv_rn(d, cell));
+  if (!(f >= 0.0f)) return 0;
+  if (f >= (float)dim) return dim - 1;
+  return (int)f;
+}
+
+__device__ __forceinline__ uint32_t leaf_key_mul(const Geometry& g, float2 inv, float x, float y) {
+  const int ix = cell_coord_mul(x, g.xmin, g.cell_x, inv.x, g.base_dim);
+  const int iy = cell_coord_mul(y, g.ymin, g.cell_y, inv.y, g.base_dim);
+  return (uint32_t)(ix + iy * g.base_dim);
+}
+
 // Outside the limits, the prune test of source/nbfmm/display/stars/prune.cu:40-41 (NaN is kept).
 __device__ __forceinline__ bool outside(const Geometry& g, float x, float y) {
   return x < g.xmin || y < g.ymin || x > g.xmax || y > g.ymax;
@@ -218,9 +238,10 @@ void launch_head(const uint32_t* keys, const int* d_n, int num_cells, int* head,
 // stays bit-identical to the same system stepped alone only if both pair alike. The item size does not change
 // any result: a pass is packed with the same neighbour pass (0-1, 2-3) and a cell's odd last pass runs alone
 // whether items hold 2 or 4 passes.
+// With head_copy, head[0..num_cells] is also copied there (the layout the next step's re-sort starts from).
 void launch_worklist(const int* head, int num_cells, int2* work, int* d_work_count, bool pair_tails,
                      cudaStream_t stream, int passes_per_item = kP2PPasses, const int* sys_cell_base = nullptr,
-                     const int* sys_passes = nullptr, int num_systems = 0);
+                     const int* sys_passes = nullptr, int num_systems = 0, int* head_copy = nullptr);
 
 // P2M on the sorted particles: leaf centres of mass summed in sorted order (predo, and the stage entry point).
 void launch_p2m(const Geometry& g, const int* head, const float4* sorted4, float4* cell0, cudaStream_t stream);
@@ -250,6 +271,8 @@ void launch_keys_from_head(const int* head, int num_cells, uint32_t* skey, cudaS
 
 enum P2PEpilogue { kStoreSorted = 0, kSolve = 1, kVerlet = 2 };
 
+constexpr uint32_t kStayFlag = 0x80000000u;  // P2PArgs::next_key: the star stays in its cell
+
 struct P2PArgs {
   const float4* sorted4;   // sorted particles
   const int* head;         // leaf heads
@@ -273,7 +296,15 @@ struct P2PArgs {
   const int* d_num_steps;
   int* d_sort_n;           // set to *d_n_import when a star leaves in the final prune
   const int* d_n_import;
-  float4 lim;              // position limits (x_min, y_min, x_max, y_max) of the final prune
+  // kVerlet, Stars: on every step but the call's last, each star's leaf key for the next step by state slot, with
+  // kStayFlag when it stays in its cell, or the dead key B*B (with its final state filed in grave) when the next
+  // step's prune removes it; null for none. next_stay[c] and next_imm[c] count the stars that stay in cell c and
+  // the live stars that move into it (both zero before the launch).
+  uint32_t* next_key;
+  int* next_stay;
+  int* next_imm;
+  Geometry geo;            // kVerlet, Stars: leaf geometry and position limits
+  float2 inv_cell;         // RN(1 / cell size) per axis (leaf_key_mul)
   // Several systems in one global leaf-cell space (batched form); num_systems == 0 for a single system.
   int num_systems;
   const int* sys_cell_base;  // [num_systems + 1] first global leaf cell of each system

@@ -389,7 +389,7 @@ __global__ void head_kernel(const uint32_t* __restrict__ keys, const int* __rest
 __global__ void worklist_kernel(const int* __restrict__ head, int num_cells, int2* __restrict__ work,
                                 int* __restrict__ d_work_count, int pair_tails, int passes_per_item,
                                 const int* __restrict__ sys_cell_base, const int* __restrict__ sys_passes,
-                                int num_systems) {
+                                int num_systems, int* __restrict__ head_copy) {
   const int lane = threadIdx.x & 31;
   // Whole warps iterate together so that the warp-wide scan below sees every lane.
   for (int base = blockIdx.x * blockDim.x; base < num_cells; base += gridDim.x * blockDim.x) {
@@ -405,6 +405,10 @@ __global__ void worklist_kernel(const int* __restrict__ head, int num_cells, int
         ppi = sys_passes[lo];
       }
       const int nt = head[c + 1] - head[c];
+      if (head_copy) {
+        head_copy[c] = head[c];
+        if (c == num_cells - 1) head_copy[num_cells] = head[num_cells];
+      }
       const bool paired = pair_tails && tails_paired(head, c);
       passes = ((paired ? nt & ~31 : nt) + 31) >> 5;
       chunks = (passes + ppi - 1) / ppi;
@@ -534,11 +538,11 @@ void launch_head(const uint32_t* keys, const int* d_n, int num_cells, int* head,
 
 void launch_worklist(const int* head, int num_cells, int2* work, int* d_work_count, bool pair_tails,
                      cudaStream_t stream, int passes_per_item, const int* sys_cell_base, const int* sys_passes,
-                     int num_systems) {
+                     int num_systems, int* head_copy) {
   cudaMemsetAsync(d_work_count, 0, sizeof(int), stream);
   worklist_kernel<<<grid_for(num_cells, 256, 152 * 8), 256, 0, stream>>>(
       head, num_cells, work, d_work_count, pair_tails ? 1 : 0, passes_per_item, sys_cell_base, sys_passes,
-      num_systems);
+      num_systems, head_copy);
 }
 
 void launch_keys_from_head(const int* head, int num_cells, uint32_t* skey, cudaStream_t stream) {

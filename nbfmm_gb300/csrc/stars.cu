@@ -10,9 +10,11 @@
 // index order (the reference's predo sorts the caller's arrays, so its cells list their stars by index; the sort
 // here starts from the previous cell order), gathers it, builds the tree and runs P2P with the L2P + Verlet
 // epilogue, which writes the new state in the new cell order.
-// Pruning is folded into the next step's key pass: a star outside the limits gets the key B*B, sorts behind
-// every live star and drops out (head[B*B] is the new count), and its final state is filed under its
-// original index together with its death step. The state of the public arrays (survivors in their previous
+// Pruning is folded into the next step's keys (the key pass of a call's first step, the P2P epilogue of the step
+// before otherwise): a star outside the limits gets the key B*B, sorts behind every live star and drops out
+// (head[B*B] is the new count), and its final state is filed under its original index together with its death
+// step. A call's first step sorts the state with the radix sort; the steps after it re-sort from the previous
+// step's cell order (below). The state of the public arrays (survivors in their previous
 // relative order, then the pruned stars, most recent first) is restored once at the end of the call.
 #include "engine.cuh"
 #include "stars.cuh"
@@ -84,6 +86,196 @@ __global__ void keys_from_state_kernel(Geometry g, StepCounters sc, const float4
     }
     keys[i] = key;
     vals[i] = (uint32_t)i;
+  }
+}
+
+// ---- Re-sort of a continuing step -----------------------------------------------------------------------------
+// Within an update call the state sits in the previous step's cell order (head_old). The previous step's P2P
+// epilogue left each star's new leaf key by state slot (kStayFlag set when the star stays in its cell; the dead
+// key B*B when the prune at the start of this step removes it) and counted, per cell, the stars that stay and the
+// live stars that move in. A step moves most stars by a small fraction of a cell, so most stay. The new cell
+// order comes from a counting sort in three short launches instead of the key pass, the radix passes and the
+// head search:
+//   resort_tile_sum_kernel, resort_head_kernel: heads = exclusive scan of stayers + immigrants per cell, each
+//     cell's first immigrant place (head + stayers), and the counts cleared for the next step's epilogue;
+//   resort_place_kernel (over the old cells): each stayer goes to its cell's head plus its rank among the cell's
+//     stayers in the old order (the order the previous step left each cell in: by index), each immigrant to a
+//     place after its new cell's stayers taken from an atomic cursor.
+// Dead stars get no place (head[B*B] is the live count). The immigrants' order depends on the atomics, but the
+// gather that follows puts every cell in index order, so the step's result does not.
+constexpr int kResortThreads = 256;
+constexpr int kResortItems = 8;                                // cells per thread in the scan
+constexpr int kResortTile = kResortThreads * kResortItems;     // cells per scan tile
+constexpr int kPlaceGroup = 16;                                // old cells per warp in resort_place_kernel
+constexpr int kPlaceUnroll = 4;                                // chunks of 32 slots whose loads are in flight
+constexpr int kMoverCap = 128;
+
+__device__ __forceinline__ int block_sum(int v, int* red) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+  __syncthreads();  // red is free
+  if (lane == 0) red[warp] = v;
+  __syncthreads();
+  int t = 0;
+  for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += red[w];
+  return t;
+}
+
+// Live stars per cell, summed over each tile of kResortTile cells.
+__global__ void __launch_bounds__(kResortThreads) resort_tile_sum_kernel(int num_cells, const int* __restrict__ stay,
+                                                                         const int* __restrict__ imm_cnt,
+                                                                         int* __restrict__ tile_sum) {
+  __shared__ int red[kResortThreads / 32];
+  const int c0 = blockIdx.x * kResortTile;
+  int v = 0;
+  for (int c = c0 + threadIdx.x; c < min(c0 + kResortTile, num_cells); c += kResortThreads) v += stay[c] + imm_cnt[c];
+  v = block_sum(v, red);
+  if (threadIdx.x == 0) tile_sum[blockIdx.x] = v;
+}
+
+// One tile per CTA: the sum of the tiles before it, then a scan of the tile's counts.
+__global__ void __launch_bounds__(kResortThreads) resort_head_kernel(int num_cells, int* __restrict__ stay,
+                                                                     int* __restrict__ imm_cnt,
+                                                                     const int* __restrict__ tile_sum,
+                                                                     int* __restrict__ head, int* __restrict__ imm_next,
+                                                                     int* __restrict__ d_n_alive) {
+  __shared__ int red[kResortThreads / 32];
+  __shared__ int warp_tot[kResortThreads / 32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  int before = 0;
+  for (int t = threadIdx.x; t < (int)blockIdx.x; t += kResortThreads) before += tile_sum[t];
+  before = block_sum(before, red);
+  const int c0 = blockIdx.x * kResortTile + threadIdx.x * kResortItems;
+  int st[kResortItems], cnt[kResortItems], mine = 0;
+#pragma unroll
+  for (int u = 0; u < kResortItems; ++u) {
+    const int c = c0 + u;
+    st[u] = c < num_cells ? stay[c] : 0;
+    cnt[u] = st[u] + (c < num_cells ? imm_cnt[c] : 0);
+    mine += cnt[u];
+  }
+  int incl = mine;
+#pragma unroll
+  for (int off = 1; off < 32; off <<= 1) {
+    const int y = __shfl_up_sync(0xffffffffu, incl, off);
+    if (lane >= off) incl += y;
+  }
+  if (lane == 31) warp_tot[warp] = incl;
+  __syncthreads();
+  int run = before + incl - mine;
+  for (int w = 0; w < warp; ++w) run += warp_tot[w];
+#pragma unroll
+  for (int u = 0; u < kResortItems; ++u) {
+    const int c = c0 + u;
+    if (c < num_cells) {
+      head[c] = run;
+      imm_next[c] = run + st[u];
+      stay[c] = 0;  // ready for the next step's epilogue
+      imm_cnt[c] = 0;
+    }
+    run += cnt[u];
+    if (c == num_cells - 1) {
+      head[num_cells] = run;
+      *d_n_alive = run;
+    }
+  }
+}
+
+struct MoverList {
+  uint32_t slot[kMoverCap];
+  uint32_t key[kMoverCap];
+};
+
+// Places the listed immigrants: one atomic per distinct new cell among 32 of them.
+__device__ __forceinline__ void place_movers(const MoverList& ml, int count, int* __restrict__ imm_next,
+                                             uint32_t* __restrict__ perm, int max_n, int lane) {
+  __syncwarp();
+  const unsigned below = (1u << lane) - 1u;
+  for (int m0 = 0; m0 < count; m0 += 32) {
+    const int j = m0 + lane;
+    const bool active = j < count;
+    const unsigned am = __ballot_sync(0xffffffffu, active);
+    if (active) {
+      const uint32_t k = ml.key[j];
+      const unsigned peers = __match_any_sync(am, k);
+      const int leader = __ffs(peers) - 1;
+      int first = 0;
+      if (lane == leader) first = atomicAdd(&imm_next[k], __popc(peers));
+      first = __shfl_sync(peers, first, leader);
+      const int at = first + __popc(peers & below);
+      if ((unsigned)at < (unsigned)max_n) perm[at] = ml.slot[j];
+    }
+  }
+  __syncwarp();
+}
+
+// A warp takes kPlaceGroup consecutive old cells, whose slots form one range starting at a cell's first slot,
+// and streams it in chunks of 32. Stayers of one cell carry their cell as key and are contiguous, so a stayer's
+// rank in its cell is the number of stayers with its key before it in the chunk, plus those counted in earlier
+// chunks when its cell continues the last stayers' cell of the chunk before. Immigrants wait in a per-warp list in
+// shared memory.
+__global__ void __launch_bounds__(kResortThreads) resort_place_kernel(int num_cells, const int* __restrict__ head_old,
+                                                                      const uint32_t* __restrict__ key,
+                                                                      const int* __restrict__ head,
+                                                                      int* __restrict__ imm_next,
+                                                                      uint32_t* __restrict__ perm, int max_n) {
+  __shared__ MoverList movers[kResortThreads / 32];
+  const int lane = threadIdx.x & 31;
+  const unsigned below = (1u << lane) - 1u;
+  MoverList& ml = movers[threadIdx.x >> 5];
+  const int groups = (num_cells + kPlaceGroup - 1) / kPlaceGroup;
+  const int warps = gridDim.x * (blockDim.x >> 5);
+  for (int grp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; grp < groups; grp += warps) {
+    const int o0 = grp * kPlaceGroup;
+    const int bound = lane < 2 ? head_old[min(o0 + lane * kPlaceGroup, num_cells)] : 0;
+    const int begin = __shfl_sync(0xffffffffu, bound, 0), end = __shfl_sync(0xffffffffu, bound, 1);
+    uint32_t carry_key = 0xffffffffu;
+    int carry = 0, nm = 0;
+    for (int base = begin; base < end; base += 32 * kPlaceUnroll) {
+      uint32_t w[kPlaceUnroll];
+      int h[kPlaceUnroll];
+#pragma unroll
+      for (int u = 0; u < kPlaceUnroll; ++u) {
+        const int i = base + 32 * u + lane;
+        w[u] = i < end ? key[i] : (uint32_t)num_cells;  // outside the range: like a dead star
+      }
+#pragma unroll
+      for (int u = 0; u < kPlaceUnroll; ++u) h[u] = (w[u] & kStayFlag) ? head[w[u] & ~kStayFlag] : 0;
+#pragma unroll
+      for (int u = 0; u < kPlaceUnroll; ++u) {
+        const int i = base + 32 * u + lane;
+        const uint32_t k = w[u] & ~kStayFlag;
+        const bool stays = (w[u] & kStayFlag) != 0;
+        const bool moves = !stays && k < (uint32_t)num_cells;
+        const unsigned sb = __ballot_sync(0xffffffffu, stays);
+        unsigned peers = 0u;
+        if (stays) {
+          peers = __match_any_sync(sb, k);
+          const int at = h[u] + __popc(peers & below) + (k == carry_key ? carry : 0);
+          if ((unsigned)at < (unsigned)max_n) perm[at] = (uint32_t)i;
+        }
+        if (sb) {  // the chunk's last stayers' cell continues into the next chunk
+          const int last = 31 - __clz(sb);
+          const uint32_t kl = __shfl_sync(0xffffffffu, k, last);
+          const int n_last = __popc(__shfl_sync(0xffffffffu, peers, last));
+          carry = (kl == carry_key ? carry : 0) + n_last;
+          carry_key = kl;
+        }
+        const unsigned mb = __ballot_sync(0xffffffffu, moves);
+        if (nm + __popc(mb) > kMoverCap) {
+          place_movers(ml, nm, imm_next, perm, max_n, lane);
+          nm = 0;
+        }
+        if (moves) {
+          const int at = nm + __popc(mb & below);
+          ml.slot[at] = (uint32_t)i;
+          ml.key[at] = k;
+        }
+        nm += __popc(mb);
+      }
+    }
+    place_movers(ml, nm, imm_next, perm, max_n, lane);
   }
 }
 
@@ -557,6 +749,18 @@ void launch_keys_from_state(const Geometry& g, const StepCounters& sc, const flo
 }
 
 void launch_finish_step(const StepCounters& sc, cudaStream_t stream) { finish_step_kernel<<<1, 1, 0, stream>>>(sc); }
+
+void launch_resort(const ResortArrays& r, int num_cells, int max_n, int* head, int* d_n_alive, cudaStream_t stream) {
+  const int tiles = (num_cells + kResortTile - 1) / kResortTile;
+  const int groups = (num_cells + kPlaceGroup - 1) / kPlaceGroup;
+  resort_tile_sum_kernel<<<tiles, kResortThreads, 0, stream>>>(num_cells, r.stay, r.imm_cnt, r.tile_sum);
+  resort_head_kernel<<<tiles, kResortThreads, 0, stream>>>(num_cells, r.stay, r.imm_cnt, r.tile_sum, head,
+                                                           r.imm_next, d_n_alive);
+  resort_place_kernel<<<grid_for((long long)groups * 32, kResortThreads, 152 * 6), kResortThreads, 0, stream>>>(
+      num_cells, r.head_old, r.key, head, r.imm_next, r.perm, max_n);
+}
+
+int resort_tiles(int num_cells) { return (num_cells + kResortTile - 1) / kResortTile; }
 
 void launch_export_fate(const StepCounters& sc, cudaStream_t stream) { export_fate_kernel<<<1, 1, 0, stream>>>(sc); }
 

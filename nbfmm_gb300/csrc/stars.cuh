@@ -45,6 +45,21 @@ void launch_keys_from_state(const Geometry& g, const StepCounters& sc, const flo
                             uint32_t dead_key, uint32_t* keys, uint32_t* vals, float4* grave, int max_n,
                             cudaStream_t stream);
 void launch_finish_step(const StepCounters& sc, cudaStream_t stream);
+
+// The cell order of a step that continues a call, from the previous step's (stars.cu, "Re-sort of a continuing
+// step"): heads, *d_n_alive = head[B*B] and perm, the state slots in the new cell order (each cell's stayers in
+// their old order, then its immigrants). The counts are cleared for the next step's P2P epilogue.
+struct ResortArrays {
+  const int* head_old;   // [num_cells + 1] the previous step's heads (the state's layout)
+  const uint32_t* key;   // [state] P2PArgs::next_key
+  int* stay;             // [num_cells] P2PArgs::next_stay, zero between steps
+  int* imm_cnt;          // [num_cells] P2PArgs::next_imm, zero between steps
+  int* imm_next;         // [num_cells] place of each cell's next immigrant
+  int* tile_sum;         // [resort_tiles(num_cells)]
+  uint32_t* perm;        // [state]
+};
+int resort_tiles(int num_cells);
+void launch_resort(const ResortArrays& r, int num_cells, int max_n, int* head, int* d_n_alive, cudaStream_t stream);
 // After the last step of an update call: notes a star lost by a step (the last step's P2P epilogue filed every
 // remaining star's final state, P2PArgs::grave).
 void launch_export_fate(const StepCounters& sc, cudaStream_t stream);

@@ -182,6 +182,42 @@ def test_grouping_of_steps_into_calls_does_not_matter(engine, level):
     assert_same_stars(a, c)
 
 
+@pytest.mark.parametrize("case", ["far", "dense", "escapes"])
+def test_continuing_steps_equal_full_sorts(engine, case):
+    """The steps after a call's first re-sort from the previous step's cell order (stayers, immigrants counted
+    per cell); a call's first step sorts in full. K steps in one call must equal K fresh handles of one step each,
+    bit for bit, when stars jump several cells per step ("far"), when one cell holds far more stars than the
+    gather stages in shared memory ("dense"), and when stars leave the limits on several steps of the call."""
+    import torch
+
+    rng = np.random.default_rng({"far": 11, "dense": 12, "escapes": 13}[case])
+    n, level, steps = 8000, 5, 6
+    cur = rng.uniform(-0.8, 0.8, (n, 2)).astype(np.float32)
+    vel = rng.uniform(-2e-3, 2e-3, (n, 2))
+    if case == "far":
+        fast = rng.choice(n, n // 10, replace=False)
+        vel[fast] = rng.uniform(-0.12, 0.12, (len(fast), 2))  # up to ~4 leaf cells (0.031) per step
+    if case == "dense":
+        cur[:1500] = rng.uniform(0.19, 0.215, (1500, 2))  # one leaf cell, (0.1875, 0.21875) on both axes
+    if case == "escapes":
+        edge = rng.choice(n, 300, replace=False)
+        cur[edge, 0] = rng.uniform(0.9, 0.99, len(edge))
+        vel[edge, 0] = rng.uniform(0.01, 0.06, len(edge))  # out after 1 to 9 steps
+    prev = (cur - vel).astype(np.float32)
+    w = (rng.uniform(0.5, 1.5, n) / n).astype(np.float32)
+    lim, tick, eps = (-1.0, -1.0, 1.0, 1.0), 1e-3, 1e-3  # the stars move by their velocities, not by the kick
+    a = make_stars(engine, cur, prev, w, level, lim, tick, eps)
+    a.update(steps)
+    c = make_stars(engine, cur, prev, w, level, lim, tick, eps)
+    for _ in range(steps):
+        c.update(1)
+        c = make_stars(engine, *arrays(c), level, lim, tick, eps)
+    torch.cuda.synchronize()
+    if case == "escapes":
+        assert n - 300 < a.num_star_ < n
+    assert_same_stars(a, c)
+
+
 @pytest.mark.parametrize("case", ["edit", "loss", "prune", "edit_then_prune"])
 def test_a_call_resumes_only_from_its_own_export(engine, case):
     """After an update call the engine keeps its state in cell order and continues from it when the public arrays
