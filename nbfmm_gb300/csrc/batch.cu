@@ -288,6 +288,8 @@ struct nbfmm_batch {
   int* level_base = nullptr;  // [max_levels][S + 1]
   int* tile_base = nullptr;   // [max_levels][S + 1]
   int* sys_passes = nullptr;  // [S] passes of 32 targets per P2P work item of each system (2 or 4)
+  int* sys_series = nullptr;  // [S] P2PArgs::series of each system for the current eps
+  std::vector<Geometry> h_geo;
   // Sort, tree and P2P workspace.
   uint32_t *keys_a = nullptr, *vals_a = nullptr, *keys_b = nullptr, *vals_b = nullptr;
   uint32_t *counts = nullptr, *digit_total = nullptr;
@@ -335,7 +337,8 @@ struct nbfmm_batch {
     n = h_off[S];
     h_levels.resize(S);
     h_dim.resize(S);
-    std::vector<Geometry> hg(S);
+    h_geo.assign(S, Geometry{});
+    std::vector<Geometry>& hg = h_geo;
     std::vector<int> h_cell_base(S + 1, 0);
     std::vector<int> h_sys_of_orig(n);
     max_levels = 1;
@@ -399,6 +402,7 @@ struct nbfmm_batch {
     BATCH_TRY(balloc(&level_base, h_level_base.size(), "level base"));
     BATCH_TRY(balloc(&tile_base, h_tile_base.size(), "tile base"));
     BATCH_TRY(balloc(&sys_passes, (size_t)S, "passes per item"));
+    BATCH_TRY(balloc(&sys_series, (size_t)S, "series flags"));
     BATCH_TRY(balloc(&keys_a, N, "keys"));
     BATCH_TRY(balloc(&vals_a, N, "values"));
     BATCH_TRY(balloc(&keys_b, N, "keys"));
@@ -464,6 +468,7 @@ struct nbfmm_batch {
     if (capture_stream) cudaStreamDestroy(capture_stream);
     bfree(geo); bfree(sys_of_orig); bfree(cell_base); bfree(dim); bfree(levels); bfree(level_base); bfree(tile_base);
     bfree(sys_passes);
+    bfree(sys_series);
     bfree(keys_a); bfree(vals_a); bfree(keys_b); bfree(vals_b); bfree(counts); bfree(digit_total);
     bfree(head); bfree(work); bfree(sorted4); bfree(sprev); bfree(cell4); bfree(ceff);
     bfree(cur); bfree(prev); bfree(w); bfree(state4); bfree(state_prev); bfree(grave); bfree(order_scratch); bfree(sys_counts);
@@ -527,6 +532,8 @@ struct nbfmm_batch {
     a.base_dim = 1;
     a.eps = eps;
     a.exact = exact;
+    a.inv_eps = 1.0f / eps;
+    a.sys_series = sys_series;
     a.ceff0 = ceff;  // level 0 = the global leaf space
     a.sprev = sprev;
     a.state4 = state4;
@@ -543,6 +550,14 @@ struct nbfmm_batch {
 
   int build_graph() {
     BATCH_TRY(alloc_head());
+    // Each system takes the series as it would stepped alone (nbfmm_solver::p2p_args).
+    std::vector<int> h_series(S);
+    for (int k = 0; k < S; ++k) {
+      h_series[k] = !exact && series_applies(h_geo[k].cell_x, h_geo[k].cell_y, eps) ? 1 : 0;
+    }
+    if (cudaMemcpy(sys_series, h_series.data(), sizeof(int) * S, cudaMemcpyHostToDevice) != cudaSuccess) {
+      return cuda_status("series flags");
+    }
     cudaGraph_t g = nullptr;
     if (cudaStreamBeginCapture(capture_stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
       return cuda_status("cudaStreamBeginCapture");

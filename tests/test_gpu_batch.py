@@ -16,6 +16,7 @@ def make_systems(seed):
         (130, 0, (-1.0, -1.0, 1.0, 1.0)),
         (5000, 5, (-1.25, -1.25, 1.25, 1.25)),
         (257, 1, (0.0, -5.0, 10.0, 5.0)),
+        (20000, 6, (-0.5, -0.5, 0.5, 0.5)),  # fine enough for the series arithmetic at eps 1e-3 (v = 0.0108)
     ]
     systems = []
     for n, level, lim in specs:
@@ -67,7 +68,7 @@ def run_batch(engine, systems, tick, eps, calls, arithmetic="fast", item_passes=
 
 
 @pytest.mark.parametrize("calls,item_passes", [([1], None), ([5], None), ([2, 3], None),
-                                               ([3], [2, 4, 2, 2, 4, 2])])
+                                               ([3], [2, 4, 2, 2, 4, 2, 2])])
 def test_batch_equals_systems_alone(engine, calls, item_passes):
     """Each system of a batch evolves bit for bit as the same system in a Stars of its own; with P2P work items of
     2 passes for some systems (the autotuner's tile choice) as well, which must not change any result."""

@@ -101,6 +101,32 @@ def test_disk_against_oracle_and_fp64(engine, orc):
     assert np.median(e_gpu) <= np.median(e_orc) * 1.001 + 1e-7
 
 
+def series_applies(limits, num_level, eps):
+    """The host rule of the fast arithmetic's reciprocal series (p2p.cu series_applies)."""
+    cell = max(limits[2] - limits[0], limits[3] - limits[1]) / 2 ** (num_level + 1)
+    return (2 * np.sqrt(2) * cell) ** 3 / eps <= 0.011
+
+
+@pytest.mark.parametrize("case", ["uniform", "clustered_with_outliers"])
+def test_series_arithmetic_meets_the_fast_rule(engine, orc, case):
+    """Where leaf cells are small against eps (r^3 << eps for every near pair), the fast arithmetic replaces
+    1 / (r^3 + eps) by a series for part of the sources in the work items away from the grid's edges; the edge
+    items, which hold the stars beyond the limits, keep the general path. Both must meet the fast-arithmetic
+    rule."""
+    rng = np.random.default_rng(21)
+    n, level, eps = 120_000, 6, 1e-2
+    lim = (-1.0, -1.0, 1.0, 1.0)
+    assert series_applies(lim, level, eps)
+    if case == "uniform":
+        pos = rng.uniform(-1, 1, (n, 2))
+    else:
+        pos = np.concatenate([rng.normal(0, 0.2, (n - 200, 2)), rng.uniform(-40, 40, (200, 2))])
+    pos = pos.astype(np.float32)
+    w = (rng.uniform(0.5, 1.5, n) / n).astype(np.float32)
+    s, eff = run_solve(engine, pos, w, level, lim, eps)
+    assert_solve_parity(eff, pos, w, level, lim, eps, orc, case=f"series {case}")
+
+
 def test_zero_particles_is_a_no_op(engine):
     import torch
 
