@@ -11,6 +11,8 @@
 //   permuteOutputVector postdo.cu:22-45    stage-alone here; fused into the P2P epilogue on the solve path
 // The cell arithmetic uses correctly rounded operations without fused multiply-add, in the reference's
 // order, so cell values round like the reference compiled for a CPU.
+#include <algorithm>
+
 #include "engine.cuh"
 
 namespace nbfmm_gb300 {
@@ -169,11 +171,17 @@ __global__ void l2p_kernel(const int* __restrict__ d_n, const uint32_t* __restri
 }
 
 // eff_origin[perm[i]] = seff[i] for kPostdoItems items per thread, all loaded before the scattered stores (a
-// grid-stride loop with one load-store round trip per iteration was latency-bound).
+// grid-stride loop with one load-store round trip per iteration was latency-bound). The stores are 8-byte
+// pieces of 32-byte sectors at random places; when the output is larger than the L2 can hold, its sectors leave
+// the L2 before their four pieces have arrived and go to DRAM several times over. So the original indices are
+// taken in windows of at most kPostdoWindowBytes of output, one launch each, every launch reading all of perm
+// and seff with evict-first loads and storing only into its window, whose sectors fill up in the L2.
 constexpr int kPostdoItems = 4;
+constexpr long long kPostdoWindowBytes = 64ll << 20;
 
 __global__ void postdo_kernel(const int* __restrict__ d_n, const uint32_t* __restrict__ perm,
-                              const float2* __restrict__ seff, float2* __restrict__ eff_origin) {
+                              const float2* __restrict__ seff, float2* __restrict__ eff_origin, uint32_t lo,
+                              uint32_t hi) {
   const int n = *d_n;
   const int base = blockIdx.x * blockDim.x * kPostdoItems + threadIdx.x;
   uint32_t p[kPostdoItems];
@@ -181,14 +189,15 @@ __global__ void postdo_kernel(const int* __restrict__ d_n, const uint32_t* __res
 #pragma unroll
   for (int k = 0; k < kPostdoItems; ++k) {
     const int i = base + k * blockDim.x;
+    p[k] = 0xffffffffu;
     if (i < n) {
-      p[k] = perm[i];
-      e[k] = seff[i];
+      p[k] = __ldcs(perm + i);
+      e[k] = __ldcs(seff + i);
     }
   }
 #pragma unroll
   for (int k = 0; k < kPostdoItems; ++k) {
-    if (base + k * (int)blockDim.x < n) eff_origin[p[k]] = e[k];
+    if (p[k] >= lo && p[k] < hi) eff_origin[p[k]] = e[k];
   }
 }
 
@@ -262,8 +271,13 @@ void launch_l2p(const int* d_n, const uint32_t* skey, const float2* ceff0, float
 
 void launch_postdo(const int* d_n, const uint32_t* perm, const float2* seff, float2* eff_origin, int max_n,
                    cudaStream_t stream) {
-  postdo_kernel<<<grid_for((long long)max_n, 256 * kPostdoItems, 1 << 30), 256, 0, stream>>>(d_n, perm, seff,
-                                                                                          eff_origin);
+  const long long windows = std::max(1ll, ((long long)max_n * 8 + kPostdoWindowBytes - 1) / kPostdoWindowBytes);
+  const long long span = ((long long)max_n + windows - 1) / windows;
+  for (long long w = 0; w < windows; ++w) {
+    const uint32_t lo = (uint32_t)(w * span), hi = (uint32_t)std::min((long long)max_n, (w + 1) * span);
+    postdo_kernel<<<grid_for((long long)max_n, 256 * kPostdoItems, 1 << 30), 256, 0, stream>>>(d_n, perm, seff,
+                                                                                              eff_origin, lo, hi);
+  }
 }
 
 }  // namespace nbfmm_gb300
