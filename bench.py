@@ -24,9 +24,21 @@ if ROOT not in sys.path:
 
 FLOP_PER_PAIR = 15  # 2 sub, 3 for r^2, 1 sqrt, 1 for r*r^2 (+eps fused: 2), 1 rcp, 1 mul by m, 4 for 2 FMAs
 SMS, FP32_LANES, MUFU_LANES = 152, 128, 16
-# Transcendental-unit operations per pair in p2p_kernel's packed passes: the square root always, the hardware
-# reciprocal on the 10 of every 16 sources whose bit is clear in NBFMM_P2P_NEWTON_MASK = 0x9249 (p2p.cu).
+# Transcendental-unit operations per pair in p2p_kernel's packed passes: the square root always, plus the
+# hardware reciprocal on the sources that do not take an FMA-pipe form -- 10 of every 16 beside the Newton
+# iteration (NBFMM_P2P_NEWTON_MASK = 0x9249), 8 of 16 beside the reciprocal series in the work items that take it
+# (NBFMM_P2P_SERIES_MASK = 0xAAAA; items away from the leaf grid's edges, when (2 sqrt(2) cell)^3 / eps is at most
+# SERIES_MAX_V, the rule of p2p.cu's series_applies).
 P2P_MUFU_PER_PAIR = 1 + 10 / 16
+P2P_MUFU_PER_PAIR_SERIES = 1 + 8 / 16
+SERIES_MAX_V = 0.011
+
+
+def series_applies(sysm, arithmetic):
+    b = 2 ** (sysm.num_level + 1)
+    lim = sysm.limits
+    cell = max(float(np.float32(lim[2] - lim[0]) / np.float32(b)), float(np.float32(lim[3] - lim[1]) / np.float32(b)))
+    return arithmetic == "fast" and sysm.epsilon > 0 and (2 * np.sqrt(2) * cell) ** 3 / sysm.epsilon <= SERIES_MAX_V
 WINDOW_CELLS = 32  # side of the CPU sample window, in leaf cells
 # DRAM bytes (read + write) of one P2P launch per particle: ncu's dram__bytes_read.sum (134.96 MB) and
 # dram__bytes_write.sum (73.99 MB) for one p2p_kernel<kVerlet> launch of the two-disk step at N = 4,194,304,
@@ -953,6 +965,8 @@ def main():
     sm_mhz = clk["sm_mhz"] or measured_sm_mhz()
     fp32_peak = SMS * FP32_LANES * 2 * sm_mhz * 1e6 / 1e12
     achieved = FLOP_PER_PAIR * pairs / p2p_s / 1e12
+    series = bool(series_applies(sysm, args.arithmetic))
+    mufu = P2P_MUFU_PER_PAIR_SERIES if series else P2P_MUFU_PER_PAIR
     out = {
         "metric": "particle-steps/s",
         "value": value,
@@ -982,8 +996,9 @@ def main():
             "flop_per_pair": FLOP_PER_PAIR, "pairs_per_launch": pairs, "p2p_ms_per_launch": p2p_s * 1e3,
             "p2p_share_of_step": p2p_ms / max(elapsed_ms, 1e-9),
             "pairs_per_s": pairs / p2p_s,
-            "mufu_ops_per_pair": P2P_MUFU_PER_PAIR,
-            "mufu_bound_pairs_per_s": SMS * MUFU_LANES * sm_mhz * 1e6 / P2P_MUFU_PER_PAIR,
+            "series": series,
+            "mufu_ops_per_pair": mufu,
+            "mufu_bound_pairs_per_s": SMS * MUFU_LANES * sm_mhz * 1e6 / mufu,
         },
         "e2e": {"value": replicas.whole_job_rate(n * e2e_steps, world, e2e_ms), "unit": "particle-steps/s",
                 "median_parts": e2e_parts, "clocks": e2e_clk,
