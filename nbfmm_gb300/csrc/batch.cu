@@ -315,13 +315,25 @@ struct nbfmm_batch {
   StepCounters sc{};
   uint32_t* skey = nullptr;
   uint32_t* perm = nullptr;
-  // Graph and profiling.
+  // The re-sort of the steps after a call's first (stars.cuh ResortArrays), over the global leaf-cell space.
+  uint32_t* step_key = nullptr;
+  uint32_t* step_perm = nullptr;
+  int* head_old = nullptr;
+  int* stay = nullptr;
+  int* imm_cnt = nullptr;
+  int* imm_next = nullptr;
+  int* tile_sum = nullptr;
+  // Graphs (a call's first step sorts in full, the others re-sort) and profiling.
+  struct StepGraph {
+    cudaGraph_t def = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    cudaGraphNode_t node_a = nullptr, node_b = nullptr;
+    int kernels = 0;
+  };
+  StepGraph first_step, next_step;
+  bool graphs_built = false;
   cudaStream_t capture_stream = nullptr;
-  cudaGraph_t graph_def = nullptr;
-  cudaGraphExec_t graph = nullptr;
   cudaEvent_t cap_a = nullptr, cap_b = nullptr;
-  cudaGraphNode_t node_a = nullptr, node_b = nullptr;
-  int kernels_per_step = 0;
   std::vector<cudaEvent_t> prof_events;
   int prof_max = 0, prof_used = 0;
 
@@ -421,6 +433,13 @@ struct nbfmm_batch {
     BATCH_TRY(balloc(&state_prev, N, "state prev"));
     BATCH_TRY(balloc(&grave, 2 * (size_t)N, "final states"));
     BATCH_TRY(balloc(&order_scratch, (size_t)kOrderScratch * N, "cell order scratch"));
+    BATCH_TRY(balloc(&step_key, N, "step keys"));
+    BATCH_TRY(balloc(&step_perm, N, "step order"));
+    BATCH_TRY(balloc(&head_old, (size_t)total_leaf + 1, "previous heads"));
+    BATCH_TRY(balloc(&stay, (size_t)total_leaf, "stayers"));
+    BATCH_TRY(balloc(&imm_cnt, (size_t)total_leaf, "immigrants"));
+    BATCH_TRY(balloc(&imm_next, (size_t)total_leaf, "immigrant places"));
+    BATCH_TRY(balloc(&tile_sum, (size_t)resort_tiles(total_leaf), "re-sort tiles"));
     BATCH_TRY(balloc(&sys_counts, (size_t)S, "system counts"));
     BATCH_TRY(balloc(&live_base, (size_t)S + 1, "live prefix"));
     BATCH_TRY(balloc(&part_off, (size_t)S + 1, "particle offsets"));
@@ -439,6 +458,8 @@ struct nbfmm_batch {
     for (int s = 0; s < S; ++s) h_counts[s] = h_off[s + 1] - h_off[s];
     cudaMemcpy(sys_counts, h_counts.data(), sizeof(int) * S, cudaMemcpyHostToDevice);
     cudaMemset(ints, 0, 16 * sizeof(int));
+    cudaMemset(stay, 0, sizeof(int) * (size_t)total_leaf);
+    cudaMemset(imm_cnt, 0, sizeof(int) * (size_t)total_leaf);
     cudaMemset(cell4, 0, sizeof(float4) * (size_t)total_cells);
     cudaMemset(ceff, 0, sizeof(float2) * (size_t)total_cells);  // systems with num_level 0 keep zero far field
     cudaMemset(cur, 0, sizeof(float2) * N);
@@ -473,6 +494,7 @@ struct nbfmm_batch {
     bfree(head); bfree(work); bfree(sorted4); bfree(sprev); bfree(cell4); bfree(ceff);
     bfree(cur); bfree(prev); bfree(w); bfree(state4); bfree(state_prev); bfree(grave); bfree(order_scratch); bfree(sys_counts);
     bfree(live_base); bfree(part_off); bfree(ints);
+    bfree(step_key); bfree(step_perm); bfree(head_old); bfree(stay); bfree(imm_cnt); bfree(imm_next); bfree(tile_sum);
   }
 
   int alloc_head() {
@@ -480,12 +502,21 @@ struct nbfmm_batch {
     return NBFMM_OK;
   }
 
+  static void drop(StepGraph& g) {
+    if (g.exec) cudaGraphExecDestroy(g.exec);
+    if (g.def) cudaGraphDestroy(g.def);
+    g = StepGraph{};
+  }
+
   void drop_graph() {
-    if (graph) cudaGraphExecDestroy(graph);
-    if (graph_def) cudaGraphDestroy(graph_def);
-    graph = nullptr;
-    graph_def = nullptr;
-    node_a = node_b = nullptr;
+    drop(first_step);
+    drop(next_step);
+    graphs_built = false;
+  }
+
+  void set_events(StepGraph& g, cudaEvent_t a, cudaEvent_t b) {
+    cudaGraphExecEventRecordNodeSetEvent(g.exec, g.node_a, a);
+    cudaGraphExecEventRecordNodeSetEvent(g.exec, g.node_b, b);
   }
 
   void drop_profile_events() {
@@ -500,15 +531,26 @@ struct nbfmm_batch {
     perm = where ? vals_b : vals_a;
   }
 
-  void enqueue_step(cudaStream_t s) {
+  // One step; a continuing step re-sorts from the previous step's cell order with the keys and counts its P2P
+  // epilogue left (stars.cu, "Re-sort of a continuing step"), the first step of a call sorts in full.
+  void enqueue_step(cudaStream_t s, bool continuing) {
     const int N = std::max(n, 1);
-    batch_keys_kernel<<<grid_for(N, 256, 152 * 16), 256, 0, s>>>(device(), sc, state4, state_prev,
-                                                                (uint32_t)total_leaf, keys_a, vals_a, grave);
-    sort(sc.n_cur, key_bits, s);
-    launch_head(skey, sc.n_cur, total_leaf, head, sc.n_alive, s);
-    launch_worklist(head, total_leaf, work, d_work_count(), true, s, kP2PPasses, cell_base, sys_passes, S);
+    const uint32_t* order = nullptr;
+    if (!continuing) {
+      batch_keys_kernel<<<grid_for(N, 256, 152 * 16), 256, 0, s>>>(device(), sc, state4, state_prev,
+                                                                  (uint32_t)total_leaf, keys_a, vals_a, grave);
+      sort(sc.n_cur, key_bits, s);
+      launch_head(skey, sc.n_cur, total_leaf, head, sc.n_alive, s);
+      order = perm;
+    } else {
+      ResortArrays r{head_old, step_key, stay, imm_cnt, imm_next, tile_sum, step_perm};
+      launch_resort(r, total_leaf, N, head, sc.n_alive, s);
+      order = step_perm;
+    }
+    launch_worklist(head, total_leaf, work, d_work_count(), true, s, kP2PPasses, cell_base, sys_passes, S, head_old);
     // gather + P2M over the global leaf space, each cell in index order
-    launch_gather_state_ordered(head, total_leaf, perm, state4, state_prev, sorted4, sprev, cell4, order_scratch, N, s);
+    launch_gather_state_ordered(head, total_leaf, order, state4, state_prev, sorted4, sprev, cell4, order_scratch, N,
+                                s);
     for (int lv = 1; lv < max_levels; ++lv) {
       if (h_level_total[lv] == 0) continue;
       batch_m2m_kernel<<<grid_for(h_level_total[lv], 256, 152 * 8), 256, 0, s>>>(
@@ -542,13 +584,62 @@ struct nbfmm_batch {
     a.num_systems = S;
     a.sys_cell_base = cell_base;
     a.sys_dim = dim;
+    a.grave = grave;  // prunes within a call; the call's final states are filed by the export
+    a.final_grave = 0;
+    a.d_step = sc.step;
+    a.d_num_steps = sc.num_steps;
+    a.next_key = step_key;
+    a.next_stay = stay;
+    a.next_imm = imm_cnt;
+    a.dead_key = (uint32_t)total_leaf;
+    a.sys_geo = geo;
     cudaEventRecordWithFlags(cap_a, s, cudaEventRecordExternal);
     launch_p2p(a, kVerlet, num_sms, s);
     cudaEventRecordWithFlags(cap_b, s, cudaEventRecordExternal);
     launch_finish_step(sc, s);
   }
 
-  int build_graph() {
+  int build_graph(StepGraph& out, bool continuing) {
+    cudaGraph_t g = nullptr;
+    if (cudaStreamBeginCapture(capture_stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+      return cuda_status("cudaStreamBeginCapture");
+    }
+    enqueue_step(capture_stream, continuing);
+    const cudaError_t e = cudaStreamEndCapture(capture_stream, &g);
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      return api_fail(NBFMM_ERR_CUDA, "batch step capture: %s", cudaGetErrorString(e));
+    }
+    const cudaError_t e2 = cudaGraphInstantiate(&out.exec, g, 0);
+    if (e2 != cudaSuccess) {
+      cudaGetLastError();
+      cudaGraphDestroy(g);
+      out.exec = nullptr;
+      return api_fail(NBFMM_ERR_CUDA, "batch step graph instantiate: %s", cudaGetErrorString(e2));
+    }
+    out.def = g;
+    size_t count = 0;
+    cudaGraphGetNodes(g, nullptr, &count);
+    std::vector<cudaGraphNode_t> nodes(count);
+    cudaGraphGetNodes(g, nodes.data(), &count);
+    out.kernels = 0;
+    for (cudaGraphNode_t nd : nodes) {
+      cudaGraphNodeType type;
+      cudaGraphNodeGetType(nd, &type);
+      if (type == cudaGraphNodeTypeKernel) ++out.kernels;
+      if (type == cudaGraphNodeTypeEventRecord) {
+        cudaEvent_t ev = nullptr;
+        cudaGraphEventRecordNodeGetEvent(nd, &ev);
+        if (ev == cap_a) out.node_a = nd;
+        if (ev == cap_b) out.node_b = nd;
+      }
+    }
+    if (!out.node_a || !out.node_b) return api_fail(NBFMM_ERR_CUDA, "batch step graph: P2P event nodes not found");
+    return cuda_status("batch step graph inspection");
+  }
+
+  int build_graphs() {
+    if (graphs_built) return NBFMM_OK;
     BATCH_TRY(alloc_head());
     // Each system takes the series as it would stepped alone (nbfmm_solver::p2p_args).
     std::vector<int> h_series(S);
@@ -558,65 +649,37 @@ struct nbfmm_batch {
     if (cudaMemcpy(sys_series, h_series.data(), sizeof(int) * S, cudaMemcpyHostToDevice) != cudaSuccess) {
       return cuda_status("series flags");
     }
-    cudaGraph_t g = nullptr;
-    if (cudaStreamBeginCapture(capture_stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
-      return cuda_status("cudaStreamBeginCapture");
+    const int rc = build_graph(first_step, false);
+    const int rc2 = rc == NBFMM_OK ? build_graph(next_step, true) : rc;
+    if (rc2 != NBFMM_OK) {
+      drop_graph();
+      return rc2;
     }
-    enqueue_step(capture_stream);
-    const cudaError_t e = cudaStreamEndCapture(capture_stream, &g);
-    if (e != cudaSuccess) {
-      cudaGetLastError();
-      return api_fail(NBFMM_ERR_CUDA, "batch step capture: %s", cudaGetErrorString(e));
-    }
-    const cudaError_t e2 = cudaGraphInstantiate(&graph, g, 0);
-    if (e2 != cudaSuccess) {
-      cudaGetLastError();
-      cudaGraphDestroy(g);
-      graph = nullptr;
-      return api_fail(NBFMM_ERR_CUDA, "batch step graph instantiate: %s", cudaGetErrorString(e2));
-    }
-    graph_def = g;
-    size_t count = 0;
-    cudaGraphGetNodes(g, nullptr, &count);
-    std::vector<cudaGraphNode_t> nodes(count);
-    cudaGraphGetNodes(g, nodes.data(), &count);
-    kernels_per_step = 0;
-    for (cudaGraphNode_t nd : nodes) {
-      cudaGraphNodeType type;
-      cudaGraphNodeGetType(nd, &type);
-      if (type == cudaGraphNodeTypeKernel) ++kernels_per_step;
-      if (type == cudaGraphNodeTypeEventRecord) {
-        cudaEvent_t ev = nullptr;
-        cudaGraphEventRecordNodeGetEvent(nd, &ev);
-        if (ev == cap_a) node_a = nd;
-        if (ev == cap_b) node_b = nd;
-      }
-    }
-    if (!node_a || !node_b) return api_fail(NBFMM_ERR_CUDA, "batch step graph: P2P event nodes not found");
-    return cuda_status("batch step graph inspection");
+    graphs_built = true;
+    return NBFMM_OK;
   }
 
   static int fate_bits(int S, int steps) { return bits_for((long long)S * (steps + 2)); }
 
   int update(int steps, cudaStream_t s) {
     if (steps <= 0 || n == 0) return NBFMM_OK;
-    if (!graph) BATCH_TRY(build_graph());
+    BATCH_TRY(build_graphs());
     const int N = std::max(n, 1);
     batch_live_scan_kernel<<<1, 1024, 0, s>>>(sys_counts, S, live_base);
     batch_import_kernel<<<grid_for(N, 256, 152 * 16), 256, 0, s>>>(device(), sc, sys_counts, live_base, cur, prev, w,
                                                                    state4, state_prev, grave, n, steps + 1);
     launch_set_int(sc.num_steps, steps, s);
     for (int k = 0; k < steps; ++k) {
+      StepGraph& g = k == 0 ? first_step : next_step;
       if (prof_used < prof_max) {
-        cudaGraphExecEventRecordNodeSetEvent(graph, node_a, prof_events[2 * prof_used]);
-        cudaGraphExecEventRecordNodeSetEvent(graph, node_b, prof_events[2 * prof_used + 1]);
+        set_events(g, prof_events[2 * prof_used], prof_events[2 * prof_used + 1]);
         ++prof_used;
       } else if (prof_max > 0 && prof_used == prof_max) {
-        cudaGraphExecEventRecordNodeSetEvent(graph, node_a, cap_a);
-        cudaGraphExecEventRecordNodeSetEvent(graph, node_b, cap_b);
+        set_events(first_step, cap_a, cap_b);
+        set_events(next_step, cap_a, cap_b);
         ++prof_used;
       }
-      if (cudaGraphLaunch(graph, s) != cudaSuccess) return cuda_status("cudaGraphLaunch");
+      if (cudaGraphLaunch(g.exec, s) != cudaSuccess) return cuda_status("cudaGraphLaunch");
     }
     batch_export_fate_kernel<<<grid_for(N, 256, 152 * 16), 256, 0, s>>>(device(), sc, state4, state_prev, grave);
     batch_fate_keys_kernel<<<grid_for(N, 256, 152 * 16), 256, 0, s>>>(device(), sc, grave, keys_a, vals_a);
@@ -734,7 +797,7 @@ int nbfmm_batch_update(nbfmm_batch* batch, int num_steps, void* stream) {
 int nbfmm_batch_profile_begin(nbfmm_batch* batch, int max_steps) {
   if (!batch) return api_fail(NBFMM_ERR_INVALID, "null batch handle");
   if (max_steps < 0) return api_fail(NBFMM_ERR_INVALID, "max_steps must be >= 0");
-  if (!batch->graph) BATCH_TRY(batch->build_graph());
+  BATCH_TRY(batch->build_graphs());
   batch->drop_profile_events();
   batch->prof_events.resize(2 * (size_t)max_steps, nullptr);
   for (auto& e : batch->prof_events) {
@@ -757,9 +820,9 @@ int nbfmm_batch_profile_end(nbfmm_batch* batch, float* p2p_ms_total, int* p2p_la
     }
     total += ms;
   }
-  if (batch->graph && batch->node_a) {
-    cudaGraphExecEventRecordNodeSetEvent(batch->graph, batch->node_a, batch->cap_a);
-    cudaGraphExecEventRecordNodeSetEvent(batch->graph, batch->node_b, batch->cap_b);
+  if (batch->graphs_built) {
+    batch->set_events(batch->first_step, batch->cap_a, batch->cap_b);
+    batch->set_events(batch->next_step, batch->cap_a, batch->cap_b);
   }
   batch->drop_profile_events();
   *p2p_ms_total = total;
@@ -773,10 +836,10 @@ int nbfmm_batch_kernel_launches(nbfmm_batch* batch, int num_steps, long long* la
     *launches = 0;
     return NBFMM_OK;
   }
-  if (!batch->graph) BATCH_TRY(batch->build_graph());
+  BATCH_TRY(batch->build_graphs());
   const int passes = (nbfmm_batch::fate_bits(batch->S, num_steps) + kRadixMaxBits - 1) / kRadixMaxBits;
   const int outside = 3 + 2 + 3 * passes + 1 + 1;  // scan, import, step count, fate, keys, sort, counts, gather
-  *launches = (long long)num_steps * batch->kernels_per_step + outside;
+  *launches = batch->first_step.kernels + (long long)(num_steps - 1) * batch->next_step.kernels + outside;
   return NBFMM_OK;
 }
 

@@ -294,26 +294,29 @@ struct P2PArgs {
   float4* state4;          // kVerlet: new state (x', y', m, original index)
   float2* state_prev;      // kVerlet: new previous positions
   float tick;              // kVerlet: tick * sqrt(G)
-  // kVerlet, Stars: the final states filed on the last step of an update call (stars.cuh file_grave); null for none.
+  // kVerlet: the final states by original index (stars.cuh file_grave), null for none: of the stars the prune at
+  // the start of the next step removes, and with final_grave (Stars) of every star on the last step of a call.
   float4* grave;
+  int final_grave;
   const int* d_step;       // 1-based step of the call, and the call's step count
   const int* d_num_steps;
   int* d_sort_n;           // set to *d_n_import when a star leaves in the final prune
   const int* d_n_import;
-  // kVerlet, Stars: on every step but the call's last, each star's leaf key for the next step by state slot, with
-  // kStayFlag when it stays in its cell, or the dead key B*B (with its final state filed in grave) when the next
-  // step's prune removes it; null for none. next_stay[c] and next_imm[c] count the stars that stay in cell c and
-  // the live stars that move into it (both zero before the launch).
+  // kVerlet: on every step but the call's last, each star's leaf key for the next step by state slot, with
+  // kStayFlag when it stays in its cell, or the dead key (B*B; dead_key in a batch) with its final state filed in
+  // grave when the next step's prune removes it; null for none. next_stay[c] and next_imm[c] count the stars that
+  // stay in cell c and the live stars that move into it (both zero before the launch).
   uint32_t* next_key;
   int* next_stay;
   int* next_imm;
-  Geometry geo;            // kVerlet, Stars: leaf geometry and position limits
-  float2 inv_cell;         // RN(1 / cell size) per axis (leaf_key_mul)
+  uint32_t dead_key;       // batch: the dead key, past the last cell of the global space
+  Geometry geo;            // kVerlet, one system: leaf geometry and position limits
   // Several systems in one global leaf-cell space (batched form); num_systems == 0 for a single system.
   int num_systems;
   const int* sys_cell_base;  // [num_systems + 1] first global leaf cell of each system
   const int* sys_dim;        // [num_systems] leaf cells per side of each system
   const int* sys_series;     // [num_systems] the series flag of each system (P2PArgs::series), or null
+  const Geometry* sys_geo;   // [num_systems] kVerlet with next_key: each system's geometry and limits
 };
 
 void launch_p2p(const P2PArgs& a, P2PEpilogue mode, int num_sms, cudaStream_t stream);
