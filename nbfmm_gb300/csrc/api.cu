@@ -398,7 +398,6 @@ struct nbfmm_stars {
     a.state_prev = state_prev;
     a.tick = tick;
     a.grave = grave;
-    a.final_grave = 1;
     a.d_step = sc.step;
     a.d_num_steps = sc.num_steps;
     a.d_sort_n = sc.sort_n;
@@ -407,6 +406,7 @@ struct nbfmm_stars {
     a.next_stay = stay;
     a.next_imm = imm_cnt;
     a.geo = v.geo;
+    a.inv_cell = make_float2(1.0f / v.geo.cell_x, 1.0f / v.geo.cell_y);
     // External records: captured as event record nodes (a plain record is only a capture-ordering marker).
     cudaEventRecordWithFlags(cap_a, s, cudaEventRecordExternal);
     launch_p2p(a, kVerlet, v.num_sms, s);

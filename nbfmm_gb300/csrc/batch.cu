@@ -289,6 +289,7 @@ struct nbfmm_batch {
   int* tile_base = nullptr;   // [max_levels][S + 1]
   int* sys_passes = nullptr;  // [S] passes of 32 targets per P2P work item of each system (2 or 4)
   int* sys_series = nullptr;  // [S] P2PArgs::series of each system for the current eps
+  float2* sys_inv = nullptr;  // [S] RN(1 / cell size) of each system (P2PArgs::sys_inv)
   std::vector<Geometry> h_geo;
   // Sort, tree and P2P workspace.
   uint32_t *keys_a = nullptr, *vals_a = nullptr, *keys_b = nullptr, *vals_b = nullptr;
@@ -415,6 +416,7 @@ struct nbfmm_batch {
     BATCH_TRY(balloc(&tile_base, h_tile_base.size(), "tile base"));
     BATCH_TRY(balloc(&sys_passes, (size_t)S, "passes per item"));
     BATCH_TRY(balloc(&sys_series, (size_t)S, "series flags"));
+    BATCH_TRY(balloc(&sys_inv, (size_t)S, "cell inverses"));
     BATCH_TRY(balloc(&keys_a, N, "keys"));
     BATCH_TRY(balloc(&vals_a, N, "values"));
     BATCH_TRY(balloc(&keys_b, N, "keys"));
@@ -445,6 +447,9 @@ struct nbfmm_batch {
     BATCH_TRY(balloc(&part_off, (size_t)S + 1, "particle offsets"));
     BATCH_TRY(balloc(&ints, 16, "counters"));
     cudaMemcpy(geo, hg.data(), sizeof(Geometry) * S, cudaMemcpyHostToDevice);
+    std::vector<float2> h_inv(S);
+    for (int s = 0; s < S; ++s) h_inv[s] = make_float2(1.0f / hg[s].cell_x, 1.0f / hg[s].cell_y);
+    cudaMemcpy(sys_inv, h_inv.data(), sizeof(float2) * S, cudaMemcpyHostToDevice);
     cudaMemcpy(sys_of_orig, h_sys_of_orig.data(), sizeof(int) * (size_t)n, cudaMemcpyHostToDevice);
     cudaMemcpy(cell_base, h_cell_base.data(), sizeof(int) * (S + 1), cudaMemcpyHostToDevice);
     const std::vector<int> h_passes(S, kP2PPasses);
@@ -490,6 +495,7 @@ struct nbfmm_batch {
     bfree(geo); bfree(sys_of_orig); bfree(cell_base); bfree(dim); bfree(levels); bfree(level_base); bfree(tile_base);
     bfree(sys_passes);
     bfree(sys_series);
+    bfree(sys_inv);
     bfree(keys_a); bfree(vals_a); bfree(keys_b); bfree(vals_b); bfree(counts); bfree(digit_total);
     bfree(head); bfree(work); bfree(sorted4); bfree(sprev); bfree(cell4); bfree(ceff);
     bfree(cur); bfree(prev); bfree(w); bfree(state4); bfree(state_prev); bfree(grave); bfree(order_scratch); bfree(sys_counts);
@@ -585,7 +591,6 @@ struct nbfmm_batch {
     a.sys_cell_base = cell_base;
     a.sys_dim = dim;
     a.grave = grave;  // prunes within a call; the call's final states are filed by the export
-    a.final_grave = 0;
     a.d_step = sc.step;
     a.d_num_steps = sc.num_steps;
     a.next_key = step_key;
@@ -593,6 +598,7 @@ struct nbfmm_batch {
     a.next_imm = imm_cnt;
     a.dead_key = (uint32_t)total_leaf;
     a.sys_geo = geo;
+    a.sys_inv = sys_inv;
     cudaEventRecordWithFlags(cap_a, s, cudaEventRecordExternal);
     launch_p2p(a, kVerlet, num_sms, s);
     cudaEventRecordWithFlags(cap_b, s, cudaEventRecordExternal);

@@ -269,7 +269,8 @@ void launch_postdo(const int* d_n, const uint32_t* perm, const float2* seff, flo
 // Sorted leaf keys from head (stage entry point helper): skey[i] = cell of i.
 void launch_keys_from_head(const int* head, int num_cells, uint32_t* skey, cudaStream_t stream);
 
-enum P2PEpilogue { kStoreSorted = 0, kSolve = 1, kVerlet = 2 };
+// kVerlet on a batch (P2PArgs::num_systems > 0) runs as kVerletBatch, whose epilogue takes each item's system.
+enum P2PEpilogue { kStoreSorted = 0, kSolve = 1, kVerlet = 2, kVerletBatch = 3 };
 
 constexpr uint32_t kStayFlag = 0x80000000u;  // P2PArgs::next_key: the star stays in its cell
 
@@ -295,9 +296,8 @@ struct P2PArgs {
   float2* state_prev;      // kVerlet: new previous positions
   float tick;              // kVerlet: tick * sqrt(G)
   // kVerlet: the final states by original index (stars.cuh file_grave), null for none: of the stars the prune at
-  // the start of the next step removes, and with final_grave (Stars) of every star on the last step of a call.
+  // the start of the next step removes, and (one system) of every star on the last step of a call.
   float4* grave;
-  int final_grave;
   const int* d_step;       // 1-based step of the call, and the call's step count
   const int* d_num_steps;
   int* d_sort_n;           // set to *d_n_import when a star leaves in the final prune
@@ -311,12 +311,14 @@ struct P2PArgs {
   int* next_imm;
   uint32_t dead_key;       // batch: the dead key, past the last cell of the global space
   Geometry geo;            // kVerlet, one system: leaf geometry and position limits
+  float2 inv_cell;         // kVerlet, one system: RN(1 / cell size) per axis (leaf_key_mul)
   // Several systems in one global leaf-cell space (batched form); num_systems == 0 for a single system.
   int num_systems;
   const int* sys_cell_base;  // [num_systems + 1] first global leaf cell of each system
   const int* sys_dim;        // [num_systems] leaf cells per side of each system
   const int* sys_series;     // [num_systems] the series flag of each system (P2PArgs::series), or null
   const Geometry* sys_geo;   // [num_systems] kVerlet with next_key: each system's geometry and limits
+  const float2* sys_inv;     // [num_systems] kVerlet with next_key: each system's RN(1 / cell size)
 };
 
 void launch_p2p(const P2PArgs& a, P2PEpilogue mode, int num_sms, cudaStream_t stream);
