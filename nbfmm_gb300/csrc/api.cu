@@ -325,6 +325,7 @@ struct nbfmm_stars {
     sc.num_steps = counters + 5;
     sc.resume = counters + 6;  // two ints; 0: the first call imports
     sc.sort_n = counters + 8;
+    sc.first_n = counters + 9;
     launch_set_int(sc.num_star, num_star, nullptr);
     if (cudaStreamCreateWithFlags(&capture_stream, cudaStreamNonBlocking) != cudaSuccess ||
         cudaEventCreate(&cap_a) != cudaSuccess || cudaEventCreate(&cap_b) != cudaSuccess) {
@@ -370,18 +371,23 @@ struct nbfmm_stars {
     delete solver;
   }
 
-  // One step: the cell order (the first step of a call: keys, sort and head; a later step: the re-sort from the
-  // previous step's order, whose P2P left the keys and did the prune), the work list, gather + P2M, far field,
-  // P2P + L2P + Verlet into the state, counters.
+  // One step: the cell order, the work list, gather + P2M, far field, P2P + L2P + Verlet into the state, counters.
+  // The steps after a call's first re-sort from the previous step's cell order, whose P2P left the keys and did
+  // the prune. A call's first step sorts in full (keys, sort, head) when the call imported its arrays, and
+  // re-sorts when it continues from the last call's state: both ways are in its graph, each doing nothing when
+  // the resume flag says the other applies.
   void enqueue_step(cudaStream_t s, bool continuing) {
     nbfmm_solver& v = *solver;
     const uint32_t* perm = nullptr;
     if (!continuing) {
       const uint32_t dead = (uint32_t)v.num_cells;
       launch_keys_from_state(v.geo, sc, state4, state_prev, dead, v.keys_a, v.vals_a, grave, max_n, s);
-      v.sort(sc.n_cur, v.key_bits, s);
-      launch_head(v.skey, sc.n_cur, v.num_cells, v.head, sc.n_alive, s);
+      v.sort(sc.first_n, v.key_bits, s);
+      launch_head(v.skey, sc.first_n, v.num_cells, v.head, sc.n_alive, s);
       perm = v.perm;
+      launch_resume_keys(v.geo, sc, v.sorted4, state4, step_key, stay, imm_cnt, max_n, s);
+      ResortArrays r{head_old, step_key, stay, imm_cnt, imm_next, tile_sum, v.perm};
+      launch_resort(r, v.num_cells, max_n, v.head, sc.n_alive, s, sc.resume);
     } else {
       ResortArrays r{head_old, step_key, stay, imm_cnt, imm_next, tile_sum, step_perm};
       launch_resort(r, v.num_cells, max_n, v.head, sc.n_alive, s);

@@ -40,6 +40,7 @@ __global__ void import_kernel(StepCounters sc, const float2* __restrict__ cur, c
     *sc.step = 1;
     *sc.prune = 0;
     if (sc.sort_n) *sc.sort_n = 0;  // raised by the export if the call loses a star
+    if (sc.first_n) *sc.first_n = copy;
   }
 }
 
@@ -72,7 +73,7 @@ __global__ void keys_from_state_kernel(Geometry g, StepCounters sc, const float4
                                        const float2* __restrict__ state_prev, uint32_t dead_key,
                                        uint32_t* __restrict__ keys, uint32_t* __restrict__ vals,
                                        float4* __restrict__ grave) {
-  const int n = *sc.n_cur;
+  const int n = sc.first_n ? *sc.first_n : *sc.n_cur;
   const int prune = *sc.prune;
   const int death_rank = *sc.num_steps + 1 - (*sc.step - 1);  // later deaths first in the final order
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
@@ -125,8 +126,10 @@ __device__ __forceinline__ int block_sum(int v, int* red) {
 // Live stars per cell, summed over each tile of kResortTile cells.
 __global__ void __launch_bounds__(kResortThreads) resort_tile_sum_kernel(int num_cells, const int* __restrict__ stay,
                                                                          const int* __restrict__ imm_cnt,
-                                                                         int* __restrict__ tile_sum) {
+                                                                         int* __restrict__ tile_sum,
+                                                                         const int* __restrict__ gate) {
   __shared__ int red[kResortThreads / 32];
+  if (gate && !*gate) return;
   const int c0 = blockIdx.x * kResortTile;
   int v = 0;
   for (int c = c0 + threadIdx.x; c < min(c0 + kResortTile, num_cells); c += kResortThreads) v += stay[c] + imm_cnt[c];
@@ -139,10 +142,19 @@ __global__ void __launch_bounds__(kResortThreads) resort_head_kernel(int num_cel
                                                                      int* __restrict__ imm_cnt,
                                                                      const int* __restrict__ tile_sum,
                                                                      int* __restrict__ head, int* __restrict__ imm_next,
-                                                                     int* __restrict__ d_n_alive) {
+                                                                     int* __restrict__ d_n_alive,
+                                                                     const int* __restrict__ gate) {
   __shared__ int red[kResortThreads / 32];
   __shared__ int warp_tot[kResortThreads / 32];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (gate && !*gate) {  // not re-sorting: only the counts are cleared
+    for (int c = blockIdx.x * kResortTile + threadIdx.x; c < min((int)(blockIdx.x + 1) * kResortTile, num_cells);
+         c += kResortThreads) {
+      stay[c] = 0;
+      imm_cnt[c] = 0;
+    }
+    return;
+  }
   int before = 0;
   for (int t = threadIdx.x; t < (int)blockIdx.x; t += kResortThreads) before += tile_sum[t];
   before = block_sum(before, red);
@@ -219,8 +231,10 @@ __global__ void __launch_bounds__(kResortThreads) resort_place_kernel(int num_ce
                                                                       const uint32_t* __restrict__ key,
                                                                       const int* __restrict__ head,
                                                                       int* __restrict__ imm_next,
-                                                                      uint32_t* __restrict__ perm, int max_n) {
+                                                                      uint32_t* __restrict__ perm, int max_n,
+                                                                      const int* __restrict__ gate) {
   __shared__ MoverList movers[kResortThreads / 32];
+  if (gate && !*gate) return;
   const int lane = threadIdx.x & 31;
   const unsigned below = (1u << lane) - 1u;
   MoverList& ml = movers[threadIdx.x >> 5];
@@ -276,6 +290,37 @@ __global__ void __launch_bounds__(kResortThreads) resort_place_kernel(int num_ce
       }
     }
     place_movers(ml, nm, imm_next, perm, max_n, lane);
+  }
+}
+
+__global__ void resume_keys_kernel(Geometry g, float2 inv, StepCounters sc, const float4* __restrict__ sorted4,
+                                   const float4* __restrict__ state4, uint32_t* __restrict__ key_word,
+                                   int* __restrict__ stay, int* __restrict__ imm_cnt) {
+  if (!sc.resume[0]) return;
+  const int n = *sc.n_cur;
+  const int lane = threadIdx.x & 31;
+  const int stride = gridDim.x * blockDim.x;
+  // Whole warps iterate together: the counts are aggregated across the lanes.
+  for (int base = blockIdx.x * blockDim.x + (threadIdx.x & ~31); base < n; base += stride) {
+    const int j = base + lane;
+    const bool valid = j < n;
+    uint32_t old_cell = 0u, key = 0u;
+    if (valid) {
+      const float4 o = sorted4[j], p = state4[j];
+      old_cell = leaf_key_mul(g, inv, o.x, o.y);
+      key = leaf_key_mul(g, inv, p.x, p.y);
+      key_word[j] = key == old_cell ? key | kStayFlag : key;
+    }
+    const bool stays = valid && key == old_cell, moves = valid && !stays;
+    const unsigned sm = __ballot_sync(0xffffffffu, stays), mm = __ballot_sync(0xffffffffu, moves);
+    if (stays) {
+      const unsigned peers = __match_any_sync(sm, key);
+      if (lane == __ffs(peers) - 1) atomicAdd(&stay[key], __popc(peers));
+    }
+    if (moves) {
+      const unsigned peers = __match_any_sync(mm, key);
+      if (lane == __ffs(peers) - 1) atomicAdd(&imm_cnt[key], __popc(peers));
+    }
   }
 }
 
@@ -750,17 +795,25 @@ void launch_keys_from_state(const Geometry& g, const StepCounters& sc, const flo
 
 void launch_finish_step(const StepCounters& sc, cudaStream_t stream) { finish_step_kernel<<<1, 1, 0, stream>>>(sc); }
 
-void launch_resort(const ResortArrays& r, int num_cells, int max_n, int* head, int* d_n_alive, cudaStream_t stream) {
+void launch_resort(const ResortArrays& r, int num_cells, int max_n, int* head, int* d_n_alive, cudaStream_t stream,
+                   const int* gate) {
   const int tiles = (num_cells + kResortTile - 1) / kResortTile;
   const int groups = (num_cells + kPlaceGroup - 1) / kPlaceGroup;
-  resort_tile_sum_kernel<<<tiles, kResortThreads, 0, stream>>>(num_cells, r.stay, r.imm_cnt, r.tile_sum);
+  resort_tile_sum_kernel<<<tiles, kResortThreads, 0, stream>>>(num_cells, r.stay, r.imm_cnt, r.tile_sum, gate);
   resort_head_kernel<<<tiles, kResortThreads, 0, stream>>>(num_cells, r.stay, r.imm_cnt, r.tile_sum, head,
-                                                           r.imm_next, d_n_alive);
+                                                           r.imm_next, d_n_alive, gate);
   resort_place_kernel<<<grid_for((long long)groups * 32, kResortThreads, 152 * 6), kResortThreads, 0, stream>>>(
-      num_cells, r.head_old, r.key, head, r.imm_next, r.perm, max_n);
+      num_cells, r.head_old, r.key, head, r.imm_next, r.perm, max_n, gate);
 }
 
 int resort_tiles(int num_cells) { return (num_cells + kResortTile - 1) / kResortTile; }
+
+void launch_resume_keys(const Geometry& g, const StepCounters& sc, const float4* sorted4, const float4* state4,
+                        uint32_t* key_word, int* stay, int* imm_cnt, int max_n, cudaStream_t stream) {
+  const float2 inv = make_float2(1.0f / g.cell_x, 1.0f / g.cell_y);
+  resume_keys_kernel<<<grid_for(max_n, 256, 152 * 8), 256, 0, stream>>>(g, inv, sc, sorted4, state4, key_word, stay,
+                                                                       imm_cnt);
+}
 
 void launch_export_fate(const StepCounters& sc, cudaStream_t stream) { export_fate_kernel<<<1, 1, 0, stream>>>(sc); }
 

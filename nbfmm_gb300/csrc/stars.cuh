@@ -17,6 +17,8 @@ struct StepCounters {
   int* resume;     // Stars only: [0] 1 when the call may continue from the state the last update call left,
                    // [1] the stars in that state (see launch_resume_check)
   int* sort_n;     // Stars only: entries the call's export sorts; 0 when it lost no star (identity export)
+  int* first_n;    // Stars only: stars the first step of a call sorts in full; 0 when the call continues from the
+                   // last call's state, which its first step re-sorts (launch_resume_keys)
 };
 
 // The final state of a star filed under its original index ("grave"): a 32-byte record of two float4,
@@ -59,7 +61,15 @@ struct ResortArrays {
   uint32_t* perm;        // [state]
 };
 int resort_tiles(int num_cells);
-void launch_resort(const ResortArrays& r, int num_cells, int max_n, int* head, int* d_n_alive, cudaStream_t stream);
+// With `gate`, nothing is re-sorted unless *gate is non-zero (the counts are cleared either way).
+void launch_resort(const ResortArrays& r, int num_cells, int max_n, int* head, int* d_n_alive, cudaStream_t stream,
+                   const int* gate = nullptr);
+// The first step of a call that continues from the last call's state (sc.resume[0] set; nothing otherwise): the
+// key word and cell counts of the re-sort, which the last call's final step did not leave. The state is in that
+// step's cell order, and its sorted copy `sorted4` still holds the positions that step was sorted by, so each
+// slot's old cell is the leaf key of sorted4 and its new cell that of state4 (no prune at a call's first step).
+void launch_resume_keys(const Geometry& g, const StepCounters& sc, const float4* sorted4, const float4* state4,
+                        uint32_t* key_word, int* stay, int* imm_cnt, int max_n, cudaStream_t stream);
 // After the last step of an update call: notes a star lost by a step (the last step's P2P epilogue filed every
 // remaining star's final state, P2PArgs::grave).
 void launch_export_fate(const StepCounters& sc, cudaStream_t stream);
