@@ -128,3 +128,36 @@ def test_batch_launch_count_and_profile(engine):
     ms, k = b.profile_end()
     assert k == 3 and ms > 0
     assert b.kernel_launches(3) > 3
+
+
+def test_batch_continuing_steps_with_far_jumps_and_a_dense_cell(engine):
+    """The steps after a call's first re-sort each system from its previous cell order with the keys the P2P
+    epilogue left in the system's own grid. Stars that jump several cells per step (or leave their system's limits)
+    and a cell holding more stars than the gather stages in shared memory must still give, system by system, the
+    same bits as the system stepped alone (whose first step sorts in full each call)."""
+    rng = np.random.default_rng(31)
+    systems = []
+    for n, level, lim in [(4000, 4, (-1.0, -1.0, 1.0, 1.0)), (3000, 5, (0.0, 0.0, 2.0, 2.0)),
+                          (2500, 3, (-3.0, -1.0, 1.0, 3.0))]:
+        lo, hi = np.array(lim[:2], np.float32), np.array(lim[2:], np.float32)
+        cur = (lo + (hi - lo) * rng.uniform(0.05, 0.95, (n, 2))).astype(np.float32)
+        vel = rng.uniform(-2e-3, 2e-3, (n, 2)) * (hi - lo)
+        fast = rng.choice(n, n // 8, replace=False)
+        vel[fast] = rng.uniform(-0.15, 0.15, (len(fast), 2)) * (hi - lo)  # several leaf cells per step
+        cur[:600] = lo + (hi - lo) * rng.uniform(0.50, 0.505, (600, 2))  # one dense cell
+        prev = (cur - vel).astype(np.float32)
+        w = (rng.uniform(0.5, 1.5, n) / n).astype(np.float32)
+        systems.append((cur, prev, w, level, lim))
+    tick, eps = 1e-3, 1e-3
+    calls = [4, 3]
+    b, off = run_batch(engine, systems, tick, eps, calls)
+    cur, pre, w = b.position_cur.cpu().numpy(), b.position_pre.cpu().numpy(), b.weight.cpu().numpy()
+    counts = b.num_stars
+    for s, (c0, p0, w0, level, lim) in enumerate(systems):
+        n, c, p, ww = run_alone(engine, c0, p0, w0, level, lim, tick, eps, calls)
+        assert counts[s] == n, f"system {s}"
+        sl = slice(off[s], off[s + 1])
+        np.testing.assert_array_equal(w[sl], ww)
+        np.testing.assert_array_equal(cur[sl], c)
+        np.testing.assert_array_equal(pre[sl], p)
+    assert sum(counts) < sum(len(s[2]) for s in systems)  # the fast stars left their limits on the way
