@@ -98,6 +98,9 @@ CONFIGS = {
     "two_disks_16m": lambda: two_disks(1 << 24, 3, 8),
     # a quarter of the particles on a quarter of the leaf cells: the same particles per cell as two_disks_16m
     "two_disks_4m": lambda: two_disks(1 << 22, 3, 7),
+    # a quarter of the particles on the same leaf cells: two_disks_16m's cell size (so P2P's reciprocal series
+    # applies as it does there), a quarter of its particles per cell
+    "two_disks_4m_fine": lambda: two_disks(1 << 22, 3, 8),
 }
 
 
