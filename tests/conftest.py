@@ -112,7 +112,7 @@ def assert_solve_parity(eff, pos, w, num_level, limits, eps, orc, tol=PARITY_TOL
     sqrt and division, no contraction) in the same order, so every effect must equal the oracle's bit for bit.
 
     arithmetic="fast" (hardware approximations): the p99.9 of the guarded relative error must be below `tol`.
-    Where the maximum is not, the north-star clause "equal or better error against the FP64 oracle" must hold:
+    Where the maximum is not, the error against the FP64 oracle must be equal or better than the oracle's:
     on the worst 32 particles plus `fp64_targets` random ones, the engine's median and maximum relative error
     against the FP64 all-pairs direct sum may exceed the oracle's by at most 0.1%. The disagreement with the
     reference's other P2P order (p2pBlock, its path for N <= 65,535 at p2p.cu:169) is recorded beside it.
