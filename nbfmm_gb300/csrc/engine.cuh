@@ -25,7 +25,10 @@ constexpr int kSortItems = 16;           // items per thread
 constexpr int kSortTile = kSortThreads * kSortItems;  // 4096 items per tile
 constexpr int kRadixMaxBits = 8;         // digit bits per pass of the (key, value) radix sort
 constexpr int kRecMaxBits = 10;          // digit bits per pass of the record sort (launch_sort_records)
-constexpr int kRecItems = 16;            // record sort: items per thread
+#ifndef NBFMM_REC_ITEMS
+#define NBFMM_REC_ITEMS 16
+#endif
+constexpr int kRecItems = NBFMM_REC_ITEMS;  // record sort: items per thread
 constexpr int kRecTile = kSortThreads * kRecItems;  // 4096 items per tile
 constexpr int kP2PThreads = 128;        // 4 independent warps per CTA
 #ifndef NBFMM_P2P_ITEM_PASSES

@@ -249,8 +249,12 @@ __host__ __device__ constexpr int rec_smem_bytes(int nd) {
   return (kSortThreads / 32) * nd * 4 + 2 * nd * 4 + kRecTile * 4 + kRecTile * 16;
 }
 
+#ifndef NBFMM_REC_MINB
+#define NBFMM_REC_MINB 2  // resident CTAs per SM the downsweep is compiled for
+#endif
+
 template <bool FROM_POS, bool FINAL>
-__global__ void __launch_bounds__(kSortThreads, 2)
+__global__ void __launch_bounds__(kSortThreads, NBFMM_REC_MINB)
 rec_downsweep_kernel(Geometry g, const float2* __restrict__ pos, const float* __restrict__ w,
                      const uint32_t* __restrict__ keys_in, const float4* __restrict__ rec_in,
                      uint32_t* __restrict__ keys_out, float4* __restrict__ rec_out, uint32_t* __restrict__ perm_out,
