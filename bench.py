@@ -26,19 +26,25 @@ FLOP_PER_PAIR = 15  # 2 sub, 3 for r^2, 1 sqrt, 1 for r*r^2 (+eps fused: 2), 1 r
 SMS, FP32_LANES, MUFU_LANES = 152, 128, 16
 # Transcendental-unit operations per pair in p2p_kernel's packed passes: the square root always, plus the
 # hardware reciprocal on the sources that do not take an FMA-pipe form -- 10 of every 16 beside the Newton
-# iteration (NBFMM_P2P_NEWTON_MASK = 0x9249), 8 of 16 beside the reciprocal series in the work items that take it
-# (NBFMM_P2P_SERIES_MASK = 0xAAAA; items away from the leaf grid's edges, when (2 sqrt(2) cell)^3 / eps is at most
-# SERIES_MAX_V, the rule of p2p.cu's series_applies).
+# iteration (NBFMM_P2P_NEWTON_MASK = 0x9249), 8 of 16 beside the degree-3 reciprocal series and 7 of 16 beside the
+# degree-2 one (NBFMM_P2P_SERIES_MASK = 0xAAAA, NBFMM_P2P_SERIES2_MASK = 0x5AB5), in the work items away from the
+# leaf grid's edges, when (2 sqrt(2) cell)^3 / eps is at most SERIES_MAX_V (degree 3) or SERIES2_MAX_V (degree 2):
+# the rule of p2p.cu's series_degree.
 P2P_MUFU_PER_PAIR = 1 + 10 / 16
-P2P_MUFU_PER_PAIR_SERIES = 1 + 8 / 16
-SERIES_MAX_V = 0.011
+P2P_MUFU_PER_PAIR_SERIES = {3: 1 + 8 / 16, 2: 1 + 7 / 16}
+SERIES_MAX_V, SERIES2_MAX_V = 0.011, 0.0062
 
 
-def series_applies(sysm, arithmetic):
+def series_degree(sysm, arithmetic):
     b = 2 ** (sysm.num_level + 1)
     lim = sysm.limits
     cell = max(float(np.float32(lim[2] - lim[0]) / np.float32(b)), float(np.float32(lim[3] - lim[1]) / np.float32(b)))
-    return arithmetic == "fast" and sysm.epsilon > 0 and (2 * np.sqrt(2) * cell) ** 3 / sysm.epsilon <= SERIES_MAX_V
+    if arithmetic != "fast" or not sysm.epsilon > 0:
+        return 0
+    v = (2 * np.sqrt(2) * cell) ** 3 / sysm.epsilon
+    return 0 if v > SERIES_MAX_V else 2 if v <= SERIES2_MAX_V else 3
+
+
 WINDOW_CELLS = 32  # side of the CPU sample window, in leaf cells
 # DRAM bytes (read + write) of one P2P launch per particle: ncu's dram__bytes_read.sum (134.96 MB) and
 # dram__bytes_write.sum (73.99 MB) for one p2p_kernel<kVerlet> launch of the two-disk step at N = 4,194,304,
@@ -965,8 +971,8 @@ def main():
     sm_mhz = clk["sm_mhz"] or measured_sm_mhz()
     fp32_peak = SMS * FP32_LANES * 2 * sm_mhz * 1e6 / 1e12
     achieved = FLOP_PER_PAIR * pairs / p2p_s / 1e12
-    series = bool(series_applies(sysm, args.arithmetic))
-    mufu = P2P_MUFU_PER_PAIR_SERIES if series else P2P_MUFU_PER_PAIR
+    series = series_degree(sysm, args.arithmetic)
+    mufu = P2P_MUFU_PER_PAIR_SERIES[series] if series else P2P_MUFU_PER_PAIR
     out = {
         "metric": "particle-steps/s",
         "value": value,
@@ -996,7 +1002,7 @@ def main():
             "flop_per_pair": FLOP_PER_PAIR, "pairs_per_launch": pairs, "p2p_ms_per_launch": p2p_s * 1e3,
             "p2p_share_of_step": p2p_ms / max(elapsed_ms, 1e-9),
             "pairs_per_s": pairs / p2p_s,
-            "series": series,
+            "series_degree": series,
             "mufu_ops_per_pair": mufu,
             "mufu_bound_pairs_per_s": SMS * MUFU_LANES * sm_mhz * 1e6 / mufu,
         },

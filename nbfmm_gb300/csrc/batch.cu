@@ -288,7 +288,7 @@ struct nbfmm_batch {
   int* level_base = nullptr;  // [max_levels][S + 1]
   int* tile_base = nullptr;   // [max_levels][S + 1]
   int* sys_passes = nullptr;  // [S] passes of 32 targets per P2P work item of each system (2 or 4)
-  int* sys_series = nullptr;  // [S] P2PArgs::series of each system for the current eps
+  int* sys_series = nullptr;  // [S] P2PArgs::series (the series degree) of each system for the current eps
   float2* sys_inv = nullptr;  // [S] RN(1 / cell size) of each system (P2PArgs::sys_inv)
   std::vector<Geometry> h_geo;
   // Sort, tree and P2P workspace.
@@ -650,7 +650,7 @@ struct nbfmm_batch {
     // Each system takes the series as it would stepped alone (nbfmm_solver::p2p_args).
     std::vector<int> h_series(S);
     for (int k = 0; k < S; ++k) {
-      h_series[k] = !exact && series_applies(h_geo[k].cell_x, h_geo[k].cell_y, eps) ? 1 : 0;
+      h_series[k] = exact ? 0 : series_degree(h_geo[k].cell_x, h_geo[k].cell_y, eps);
     }
     if (cudaMemcpy(sys_series, h_series.data(), sizeof(int) * S, cudaMemcpyHostToDevice) != cudaSuccess) {
       return cuda_status("series flags");

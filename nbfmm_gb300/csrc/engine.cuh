@@ -287,8 +287,8 @@ struct P2PArgs {
   int base_dim;
   float eps;
   int exact;               // 1: correctly rounded kernelFunction, no contraction (NBFMM_ARITH_EXACT)
-  // Fast arithmetic: 1 when the reciprocal series may replace 1 / (r^3 + eps) in the items away from the leaf
-  // grid's edges (series_applies), with inv_eps = RN(1 / eps).
+  // Fast arithmetic: the degree of the reciprocal series that may replace 1 / (r^3 + eps) in the items away from
+  // the leaf grid's edges (series_degree), 0 for none; inv_eps = RN(1 / eps).
   int series;
   float inv_eps;
   const float2* ceff0;     // level-0 local effects (kSolve, kVerlet), may be null when num_level == 0
@@ -319,16 +319,16 @@ struct P2PArgs {
   int num_systems;
   const int* sys_cell_base;  // [num_systems + 1] first global leaf cell of each system
   const int* sys_dim;        // [num_systems] leaf cells per side of each system
-  const int* sys_series;     // [num_systems] the series flag of each system (P2PArgs::series), or null
+  const int* sys_series;     // [num_systems] the series degree of each system (P2PArgs::series), or null
   const Geometry* sys_geo;   // [num_systems] kVerlet with next_key: each system's geometry and limits
   const float2* sys_inv;     // [num_systems] kVerlet with next_key: each system's RN(1 / cell size)
 };
 
 void launch_p2p(const P2PArgs& a, P2PEpilogue mode, int num_sms, cudaStream_t stream);
 
-// Whether the series arithmetic of p2p.cu is accurate for a leaf grid of these cell sizes and this eps: the
-// farthest pair of an item whose neighbourhood avoids the grid's edges is 2 sqrt(2) cells apart, and its
-// v = r^3 / eps must stay below the bound for which four terms reach 2^-26.
-bool series_applies(float cell_x, float cell_y, float eps);
+// The series arithmetic of p2p.cu for a leaf grid of these cell sizes and this eps: the farthest pair of an item
+// whose neighbourhood avoids the grid's edges is 2 sqrt(2) cells apart, and its v = r^3 / eps decides the degree
+// of the series that stays within its error bound: 2, 3, or 0 where neither applies.
+int series_degree(float cell_x, float cell_y, float eps);
 
 }  // namespace nbfmm_gb300

@@ -198,7 +198,7 @@ struct nbfmm_solver {
     a.base_dim = geo.base_dim;
     a.eps = eps;
     a.exact = exact;
-    a.series = !exact && series_applies(geo.cell_x, geo.cell_y, eps) ? 1 : 0;
+    a.series = exact ? 0 : series_degree(geo.cell_x, geo.cell_y, eps);
     a.inv_eps = 1.0f / eps;
     a.ceff0 = geo.num_level > 0 ? ceff0() : nullptr;
     return a;
