@@ -26,13 +26,12 @@ FLOP_PER_PAIR = 15  # 2 sub, 3 for r^2, 1 sqrt, 1 for r*r^2 (+eps fused: 2), 1 r
 SMS, FP32_LANES, MUFU_LANES = 152, 128, 16
 # Transcendental-unit operations per pair in p2p_kernel's packed passes: the square root always, plus the
 # hardware reciprocal on the sources that do not take an FMA-pipe form -- 10 of every 16 beside the Newton
-# iteration (NBFMM_P2P_NEWTON_MASK = 0x9249), 8 of 16 beside the degree-3 reciprocal series and 7 of 16 beside the
-# degree-2 one (NBFMM_P2P_SERIES_MASK = 0xAAAA, NBFMM_P2P_SERIES2_MASK = 0x5AB5), in the work items away from the
-# leaf grid's edges, when (2 sqrt(2) cell)^3 / eps is at most SERIES_MAX_V (degree 3) or SERIES2_MAX_V (degree 2):
-# the rule of p2p.cu's series_degree.
+# iteration (NBFMM_P2P_NEWTON_MASK = 0x9249), 7 of 16 beside the degree-2 reciprocal series
+# (NBFMM_P2P_SERIES_MASK = 0x5AB5) in the work items away from the leaf grid's edges, when
+# (2 sqrt(2) cell)^3 / eps is at most SERIES_MAX_V: the rule of p2p.cu's series_degree.
 P2P_MUFU_PER_PAIR = 1 + 10 / 16
-P2P_MUFU_PER_PAIR_SERIES = {3: 1 + 8 / 16, 2: 1 + 7 / 16}
-SERIES_MAX_V, SERIES2_MAX_V = 0.011, 0.0062
+P2P_MUFU_PER_PAIR_SERIES = {2: 1 + 7 / 16}
+SERIES_MAX_V = 0.0062
 
 
 def series_degree(sysm, arithmetic):
@@ -41,8 +40,7 @@ def series_degree(sysm, arithmetic):
     cell = max(float(np.float32(lim[2] - lim[0]) / np.float32(b)), float(np.float32(lim[3] - lim[1]) / np.float32(b)))
     if arithmetic != "fast" or not sysm.epsilon > 0:
         return 0
-    v = (2 * np.sqrt(2) * cell) ** 3 / sysm.epsilon
-    return 0 if v > SERIES_MAX_V else 2 if v <= SERIES2_MAX_V else 3
+    return 2 if (2 * np.sqrt(2) * cell) ** 3 / sysm.epsilon <= SERIES_MAX_V else 0
 
 
 WINDOW_CELLS = 32  # side of the CPU sample window, in leaf cells

@@ -328,7 +328,7 @@ void launch_p2p(const P2PArgs& a, P2PEpilogue mode, int num_sms, cudaStream_t st
 
 // The series arithmetic of p2p.cu for a leaf grid of these cell sizes and this eps: the farthest pair of an item
 // whose neighbourhood avoids the grid's edges is 2 sqrt(2) cells apart, and its v = r^3 / eps decides the degree
-// of the series that stays within its error bound: 2, 3, or 0 where neither applies.
+// of the series that stays within its error bound: 2, or 0 where it does not apply.
 int series_degree(float cell_x, float cell_y, float eps);
 
 }  // namespace nbfmm_gb300

@@ -16,7 +16,7 @@ def make_systems(seed):
         (130, 0, (-1.0, -1.0, 1.0, 1.0)),
         (5000, 5, (-1.25, -1.25, 1.25, 1.25)),
         (257, 1, (0.0, -5.0, 10.0, 5.0)),
-        (20000, 6, (-0.5, -0.5, 0.5, 0.5)),  # fine enough for the series arithmetic at eps 1e-3 (v = 0.0108)
+        (20000, 7, (-0.5, -0.5, 0.5, 0.5)),  # fine enough for the series arithmetic at eps 1e-3 (v = 0.0014)
     ]
     systems = []
     for n, level, lim in specs:

@@ -104,21 +104,19 @@ def test_disk_against_oracle_and_fp64(engine, orc):
 def series_degree(limits, num_level, eps):
     """The host rule of the fast arithmetic's reciprocal series (p2p.cu series_degree)."""
     cell = max(limits[2] - limits[0], limits[3] - limits[1]) / 2 ** (num_level + 1)
-    v = (2 * np.sqrt(2) * cell) ** 3 / eps
-    return 0 if v > 0.011 else 2 if v <= 0.0062 else 3
+    return 2 if (2 * np.sqrt(2) * cell) ** 3 / eps <= 0.0062 else 0
 
 
-@pytest.mark.parametrize("degree", [3, 2])
 @pytest.mark.parametrize("case", ["uniform", "clustered_with_outliers"])
-def test_series_arithmetic_meets_the_fast_rule(engine, orc, case, degree):
+def test_series_arithmetic_meets_the_fast_rule(engine, orc, case):
     """Where leaf cells are small against eps (r^3 << eps for every near pair), the fast arithmetic replaces
-    1 / (r^3 + eps) by a series of degree 3 (or 2 where r^3 / eps is smaller still) for part of the sources in
-    the work items away from the grid's edges; the edge items, which hold the stars beyond the limits, keep the
+    1 / (r^3 + eps) by a series of degree 2 for part of the sources in the work items away from the grid's
+    edges; the edge items, which hold the stars beyond the limits, keep the
     general path. Both must meet the fast-arithmetic rule."""
     rng = np.random.default_rng(21)
-    n, level, eps = 120_000, 6, {3: 1e-2, 2: 2e-2}[degree]
+    n, level, eps = 120_000, 6, 2e-2
     lim = (-1.0, -1.0, 1.0, 1.0)
-    assert series_degree(lim, level, eps) == degree
+    assert series_degree(lim, level, eps) == 2
     if case == "uniform":
         pos = rng.uniform(-1, 1, (n, 2))
     else:
@@ -126,7 +124,7 @@ def test_series_arithmetic_meets_the_fast_rule(engine, orc, case, degree):
     pos = pos.astype(np.float32)
     w = (rng.uniform(0.5, 1.5, n) / n).astype(np.float32)
     s, eff = run_solve(engine, pos, w, level, lim, eps)
-    assert_solve_parity(eff, pos, w, level, lim, eps, orc, case=f"series{degree} {case}")
+    assert_solve_parity(eff, pos, w, level, lim, eps, orc, case=f"series {case}")
 
 
 def test_zero_particles_is_a_no_op(engine):

@@ -182,7 +182,7 @@ def test_grouping_of_steps_into_calls_does_not_matter(engine, level):
     assert_same_stars(a, c)
 
 
-@pytest.mark.parametrize("case", ["far", "dense", "escapes", "series", "series2"])
+@pytest.mark.parametrize("case", ["far", "dense", "escapes", "series"])
 def test_continuing_steps_equal_full_sorts(engine, case):
     """The steps after a call's first re-sort from the previous step's cell order (stayers, immigrants counted
     per cell); a call's first step sorts in full. K steps in one call must equal K fresh handles of one step each,
@@ -190,11 +190,11 @@ def test_continuing_steps_equal_full_sorts(engine, case):
     gather stages in shared memory ("dense"), and when stars leave the limits on several steps of the call."""
     import torch
 
-    rng = np.random.default_rng({"far": 11, "dense": 12, "escapes": 13, "series": 14, "series2": 15}[case])
+    rng = np.random.default_rng({"far": 11, "dense": 12, "escapes": 13, "series": 15}[case])
     n, level, steps = 8000, 5, 6
     eps = 1e-3
-    if case.startswith("series"):  # leaf cells small enough for the fast arithmetic's reciprocal series
-        n, level, eps = 30000, 6, 1e-2 if case == "series" else 2e-2  # degree 3, degree 2
+    if case == "series":  # leaf cells small enough for the fast arithmetic's reciprocal series
+        n, level, eps = 30000, 6, 2e-2
     cur = rng.uniform(-0.8, 0.8, (n, 2)).astype(np.float32)
     vel = rng.uniform(-2e-3, 2e-3, (n, 2))
     if case == "far":
