@@ -103,7 +103,8 @@ __global__ void keys_from_state_kernel(Geometry g, StepCounters sc, const float4
 //     stayers in the old order (the order the previous step left each cell in: by index), each immigrant to a
 //     place after its new cell's stayers taken from an atomic cursor.
 // Dead stars get no place (head[B*B] is the live count). The immigrants' order depends on the atomics, but the
-// gather that follows puts every cell in index order, so the step's result does not.
+// gather that follows puts every cell in index order, so the step's result does not. The first step of a call that
+// continues from the last call's state re-sorts too, with the key word and counts of resume_keys_kernel.
 constexpr int kResortThreads = 256;
 constexpr int kResortItems = 8;                                // cells per thread in the scan
 constexpr int kResortTile = kResortThreads * kResortItems;     // cells per scan tile
