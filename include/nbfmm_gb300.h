@@ -49,8 +49,10 @@ int nbfmm_solver_set_epsilon(nbfmm_solver* solver, float epsilon);
 /* Arithmetic of the near field (P2P), per handle. No counterpart in the reference, whose kernelFunction
  * (include/nbfmm/core/kernel_function.hpp:36-39) uses IEEE sqrt and division.
  *   NBFMM_ARITH_FAST (default): hardware square-root and reciprocal approximations and fused multiply-adds, in
- *     the reference's p2pNaive summation order; effects differ from IEEE evaluation in the last bits of each
- *     pair, which cancellation can raise above 1e-5 relative on particles whose field nearly cancels.
+ *     the reference's p2pNaive summation order; where leaf cells are small against eps ((2 sqrt(2) cell)^3 / eps
+ *     <= 0.0062), part of the reciprocals 1 / (r^3 + eps) are the series (1 / eps)(1 - v + v^2), v = r^3 / eps.
+ *     Effects differ from IEEE evaluation in the last bits of each pair, which cancellation can raise above 1e-5
+ *     relative on particles whose field nearly cancels.
  *   NBFMM_ARITH_EXACT: every operation of kernelFunction's source rounded once, with correctly rounded sqrt and
  *     division and no fused multiply-add, summed in p2pNaive order (p2p.cu:49-66): the effects round exactly
  *     like the reference's algorithm evaluated in IEEE single precision. Slower near field. */
